@@ -1,0 +1,337 @@
+"""Throughput of the GB300 kNN-graph build (vectors/s) on synthetic SISAP-shaped data.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config full|1m|small]
+    python bench.py --impl reference ...     # the reference's CPU path (oracle port)
+
+A step is one whole graph build of one synthetic dataset (quantise, RP forest,
+leaf init, NN-Descent to the reference's early stop, export): the stages
+Aftab5550/SISAP-2026-task1 src/main.cpp:179-457 runs.  `value` is vectors/s
+with the float32 rows already in HBM (device-timed with CUDA events on the
+library's stream); `e2e` is the same build through knng_build with pinned host
+rows in and host knns/dists out, copies inside the timed region.  The inputs
+(26 GB at 6.35M x 1024) are far larger than L2, so no flush is needed.
+
+Several GPUs run independent replicas (the build does not shard): each rank
+builds its own dataset of the configured size; value = all ranks' vectors /
+max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "sisap-2026-task1_gb300")
+sys.path.insert(0, PKG)
+
+CONFIGS = {
+    # name: (n, d, centres, description)
+    "full": (6_350_000, 1024, 50_000, "full-scale single build 6.35M x 1024, 50k centres"),
+    "1m": (1_000_000, 1024, 10_000, "single build 1M x 1024, 10k centres"),
+    "small": (100_000, 1024, 1_000, "plain small 100k x 1024, 1k centres"),
+}
+CPU_SAMPLE = (100_000, 1024, 1_000)  # bounded CPU sample (the 100k small config), ~10-30 s of CPU work
+METRIC = "vectors/s (kNN-graph build, recall@15-checked)"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Group:
+    """Barrier and max-over-ranks for N independent replicas (no data-path collective)."""
+
+    def __init__(self, backend):
+        self.ws, self.rank, self.local = dist_env()
+        self.dist = None
+        if self.ws > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v, device=None):
+        if not self.dist:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+def recall_sample(x, knns, rows=10_000, seed=7):
+    """recall@15 of exported knns on a seeded row sample vs exact fp64 brute force (GPU)."""
+    import torch
+
+    import synth
+
+    n = x.shape[0]
+    g = torch.Generator().manual_seed(seed)
+    idx = torch.randperm(n, generator=g)[: min(rows, n)].to(x.device)
+    gt = []
+    for s in range(0, len(idx), 1000):
+        q = idx[s:s + 1000]
+        sims = x[q] @ x.T  # fp32 pass, then fp64 rescoring of the best 64
+        sims[torch.arange(len(q), device=x.device), q] = -float("inf")
+        cand = sims.topk(64, dim=1).indices
+        exact = torch.einsum("bd,bmd->bm", x[q].double(), x[cand].double())
+        exact[cand == q[:, None]] = -float("inf")
+        order = exact.argsort(dim=1, descending=True, stable=True)[:, :15]
+        gt.append(torch.gather(cand, 1, order).cpu())
+        del sims
+    gt = torch.cat(gt).numpy()
+    kh = knns.cpu().numpy() if hasattr(knns, "cpu") else knns
+    return synth.recall_at_k(kh, gt, rows=idx.cpu().numpy())
+
+
+def cpu_port_step(threads, sample=CPU_SAMPLE, seed=4242):
+    """One reference-algorithm build (oracle port, OpenMP) on the bounded sample; returns (s, n)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import synth
+
+    n, d, c = sample
+    x = synth.mixture(n, d, c, seed=seed)
+    prm = oracle.params(threads=threads)
+    t0 = time.perf_counter()
+    oracle.build_graph(x, prm)
+    return time.perf_counter() - t0, n
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    cfg = CONFIGS[args.config]
+    times = []
+    for k in range(args.warmup + args.steps):
+        s, n = cpu_port_step(threads)
+        if k >= args.warmup:
+            times.append(s)
+    v = CPU_SAMPLE[0] / statistics.mean(times)
+    sample = f"{CPU_SAMPLE[0]} x {CPU_SAMPLE[1]} rows, {CPU_SAMPLE[2]} centres, same generator; whole build per step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "vectors/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8/int32",
+        "data": "synthetic", "config": {"workload": cfg[3], "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "vectors/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "vectors/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference src/main.cpp needs libhdf5 and cannot run on this host; its restatement (oracle/knng_oracle.cpp, pinned bit-exact to the reference binary) runs with OpenMP",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    import knng
+    import synth
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    grp = Group("nccl" if ws > 1 else "gloo")
+    n, d, centres, desc = CONFIGS[args.config]
+    dev = torch.device("cuda", local)
+    x = synth.mixture_torch(n, d, centres, seed=1000 * 2 + rank, device=dev)
+    torch.cuda.synchronize()
+    prm = knng.params(device=local)
+    ctx = knng.Context(prm)
+    knns = torch.empty((n, prm.k_eval), dtype=torch.int32, device=dev)
+    dists = torch.empty((n, prm.k_eval), dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        ctx.build(x, knns, dists)
+    # ---- device-resident timed region
+    stats = []
+    grp.barrier()
+    torch.cuda.synchronize()
+    launches = 0
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st = knng.Stats()
+            ctx.build(x, knns, dists, st)
+            stats.append(st)
+            launches += st.kernel_launches
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    grp.barrier()
+    dev_s = sum(s.device_s for s in stats)
+    t_max = grp.max(dev_s, device=dev)
+    ms_per_step = 1e3 * t_max / args.steps
+    value = ws * n * args.steps / t_max
+    # ---- end to end: pinned host rows in, host knns/dists out
+    e2e = None
+    if not args.skip_e2e:
+        xh = torch.empty((n, d), dtype=torch.float32, pin_memory=True)
+        xh.copy_(x)
+        kh = torch.empty((n, prm.k_eval), dtype=torch.int32, pin_memory=True)
+        dh = torch.empty((n, prm.k_eval), dtype=torch.float32, pin_memory=True)
+        ctx.build(xh, kh, dh)  # warm the host-input path
+        grp.barrier()
+        e2e_s = 0.0
+        for _ in range(args.steps):
+            st = knng.Stats()
+            ctx.build(xh, kh, dh, st)
+            e2e_s += st.device_s
+        e2e_max = grp.max(e2e_s, device=dev)
+        e2e = {"value": ws * n * args.steps / e2e_max, "unit": "vectors/s", "h2d_bytes_per_step": n * d * 4,
+               "d2h_bytes_per_step": n * prm.k_eval * 8}
+        del xh
+    # ---- roofline of the dominant kernel (NN-Descent join launches)
+    last = stats[-1]
+    it = last.iterations
+    join_ms = [last.join_ms[i] for i in range(it)]
+    K = prm.k_build
+    W8 = d // 8
+    alg_bytes = []
+    for i in range(it):
+        rows_b = n * (K * 8 + K * K * 4 + d + W8 + K * 8)  # own list, 2-hop ids, own row+sketch, list write
+        alg_bytes.append(rows_b + last.join_candidates[i] * W8 + last.join_dots[i] * d)
+    peak, peak_kind = load_peaks()
+    achieved = sum(alg_bytes) / (sum(join_ms) * 1e-3) / 1e9 if it else 0.0
+    roofline = {"kernel": "join_kernel (NN-Descent iteration)", "bound": "hbm", "achieved": achieved,
+                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "alg_bytes_per_launch": sum(alg_bytes) / max(1, it),
+                "ms_per_launch": sum(join_ms) / max(1, it)}
+    if args.traffic_per_launch:
+        roofline["traffic"] = args.traffic_per_launch
+    # ---- recall on a seeded sample
+    rec = recall_sample(x, knns, rows=args.recall_rows) if args.recall_rows > 0 and rank == 0 else None
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        threads = os.cpu_count() or 1
+        s, ns = cpu_port_step(threads)
+        cpu = {"value": ns / s, "unit": "vectors/s", "cores": threads, "kind": "port",
+               "sample": f"{CPU_SAMPLE[0]} x {CPU_SAMPLE[1]} rows ({CPU_SAMPLE[2]} centres), one whole build, "
+                         "oracle restatement of src/main.cpp with OpenMP"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "vectors/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int8/int32", "data": "synthetic (seeded Gaussian mixture, Zipf 1.1)",
+            "config": {"workload": desc, "n": n, "d": d, "centres": centres, "k": prm.k_eval,
+                       "k_build": K, "trees": prm.num_trees, "leaf": prm.leaf_size, "rerank": prm.rerank_mult,
+                       "join": "jacobi" if prm.join_mode == 0 else "inplace",
+                       "l2": "inputs (n x d float32) far larger than L2; no flush",
+                       "parallelism": f"replicas x{ws}"},
+            "build_s": last.build_s, "step_s": last.device_s, "iterations": it,
+            "stage_s": {"quantize": last.quantize_s, "forest": last.forest_s, "init": last.init_s,
+                        "join": last.join_s, "export": last.export_s},
+            "recall@15": rec, "recall_rows": args.recall_rows,
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clk.summary(), "gpu_launches": launches, "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    grp.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--config", default="full", choices=sorted(CONFIGS))
+    ap.add_argument("--recall-rows", type=int, default=10_000)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--traffic-per-launch", type=float, default=None,
+                    help="dram read+write bytes per join launch from an ncu capture, scaled to this workload")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gpu":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,154 @@
+/* knng.h -- C ABI of the GB300 kNN-graph builder (libknng.so).
+ *
+ * Drop-in for the compute core of Aftab5550/SISAP-2026-task1 src/main.cpp.
+ * The reference has no library or FFI: its only interface is the process
+ * (`main --task T --dataset F`, src/main.cpp:114-141) that reads /train
+ * (src/main.cpp:149-177), builds the graph (src/main.cpp:179-457) and writes
+ * knns/dists (src/main.cpp:459-480).  These entry points replace the code
+ * between reading /train and writing the result file; the knng_main CLI keeps
+ * the reference's argv, messages and output file on top of them.
+ *
+ * Conventions: every call returns 0 (KNNG_OK) or a negative knng_status; no
+ * C++ exception crosses this boundary.  The caller owns every input and
+ * output buffer; a knng_ctx owns its device memory and CUDA stream.  A ctx is
+ * used by one host thread at a time.  Pointers marked _dev are device
+ * pointers; `stream` arguments are cudaStream_t passed as void* (NULL = the
+ * legacy default stream).
+ */
+#ifndef KNNG_H_
+#define KNNG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return codes.  The reference returns -1 on every failure
+ * (src/main.cpp:140, 197, 200, 484, 487); these refine that -1. */
+typedef enum knng_status {
+  KNNG_OK = 0,
+  KNNG_E_ARGS = -1,    /* bad argument (null pointer, n < 2, bad parameter) */
+  KNNG_E_DIM = -2,     /* d must be a multiple of 128 in [128, 1024] */
+  KNNG_E_OOM = -3,     /* device allocation failed */
+  KNNG_E_ADMIT = -4,   /* job refused by the memory-footprint admission */
+  KNNG_E_TIMEOUT = -5, /* a bounded device wait gave up */
+  KNNG_E_CUDA = -6,    /* CUDA runtime error (message: knng_last_error) */
+  KNNG_E_REPLAY = -7,  /* replay pivot table does not match the forest */
+  KNNG_E_BUSY = -8,    /* ticket not finished yet (knng_poll) */
+  KNNG_E_NOTFOUND = -9 /* unknown ticket */
+} knng_status;
+
+enum { KNNG_QUANT_TRUNC = 0, KNNG_QUANT_ROUND = 1 };
+enum { KNNG_JOIN_JACOBI = 0, KNNG_JOIN_INPLACE = 1 };
+enum { KNNG_ORDER_NATURAL = 0, KNNG_ORDER_LEAF = 1 };
+
+/* Build parameters.  Defaults (knng_default_params) are the reference's
+ * compile-time constants, src/main.cpp:19-29. */
+typedef struct knng_params {
+  int k_build;           /* K_BUILD = 50           src/main.cpp:22 */
+  int k_eval;            /* K_EVAL = 15            src/main.cpp:21 */
+  int num_trees;         /* NUM_TREES = 16         src/main.cpp:23 */
+  int rerank_mult;       /* RERANK_MULTIPLIER = 8  src/main.cpp:24 */
+  int leaf_size;         /* LEAF_SIZE = 64         src/main.cpp:25 */
+  int max_iterations;    /* MAX_ITERATIONS = 30    src/main.cpp:27 */
+  float early_stop_rate; /* EARLY_STOP_RATE = 0.04 src/main.cpp:28 */
+  float rate_diff_tol;   /* RATE_DIFF_TOLERANCE = 0.01 src/main.cpp:29 */
+  int quant_mode;        /* KNNG_QUANT_TRUNC: src/main.cpp:184-186 */
+  int join_mode;         /* KNNG_JOIN_JACOBI (deterministic) or _INPLACE */
+  int row_order;         /* KNNG_ORDER_LEAF: process rows in tree-0 leaf order */
+  uint32_t seed;         /* 1337: src/main.cpp:210 (trees), :271 (fills) */
+  int device;            /* CUDA device ordinal */
+} knng_params;
+
+/* Per-build timings and convergence record (seconds, device-timed). */
+typedef struct knng_stats {
+  double quantize_s;  /* H2D copy + quantise/sketch (outside build_s, as :203) */
+  double forest_s;    /* RP forest                 src/main.cpp:205-218 */
+  double init_s;      /* leaf Gram + top-K init    src/main.cpp:220-316 */
+  double join_s;      /* NN-Descent iterations     src/main.cpp:318-440 */
+  double export_s;    /* top-k_eval export + D2H   src/main.cpp:445-457 */
+  double build_s;     /* forest + init + join, the reference's buildtime */
+  double total_s;     /* whole knng_build call */
+  int iterations;     /* NN-Descent iterations run */
+  int64_t updates[64];/* per-iteration update counts (src/main.cpp:433) */
+  int64_t forest_levels;
+  int64_t leaves;
+  double device_s;        /* first to last device event of the call */
+  double join_ms[64];     /* device time of each NN-Descent launch */
+  int64_t join_candidates[64]; /* sketch candidates scored per iteration */
+  int64_t join_dots[64];  /* int8 rows reranked per iteration */
+  int64_t kernel_launches;/* libknng kernels launched by the call */
+} knng_stats;
+
+typedef struct knng_ctx knng_ctx;
+
+/* Fill *p with the reference defaults (src/main.cpp:19-29). */
+void knng_default_params(knng_params* p);
+
+/* Create a context on p->device.  Replaces the reference's process start-up
+ * and array allocation, src/main.cpp:143-163. */
+int knng_create(knng_ctx** out, const knng_params* p);
+
+/* Release the context and all its device memory. */
+void knng_destroy(knng_ctx* ctx);
+
+/* Build the all-points kNN graph of n rows of d float32 (row-major).
+ * Replaces src/main.cpp:179-457 (quantise, forest, init, NN-Descent, export).
+ * rows      : host or device pointer (rows_on_device selects).
+ * knns      : n * k_eval int32, 1-based ids, each row worst -> best
+ *             (src/main.cpp:452, 455).
+ * dists     : n * k_eval float32 int8 inner products, same order (:453, 456).
+ * out_on_device selects whether knns/dists are device pointers.
+ * stats may be NULL. */
+int knng_build(knng_ctx* ctx, const void* rows, int64_t n, int d, int rows_on_device,
+               int32_t* knns, float* dists, int out_on_device, knng_stats* stats);
+
+/* Text for a status code, and the last detailed error message of ctx. */
+const char* knng_status_string(int status);
+const char* knng_last_error(const knng_ctx* ctx);
+
+/* ---- stage entry points (device pointers; used by the parity tests) ---- */
+
+/* a1, src/main.cpp:179-192: int8 codes [n][d] and sign sketches [n][d/64]
+ * (bit k%64 of word k/64 set iff the clamped value is > 0). */
+int knng_quantize(const float* x_dev, int64_t n, int d, int quant_mode, int8_t* codes_dev,
+                  uint64_t* sketch_dev, void* stream);
+
+/* a2/a3, src/main.cpp:47-99, 205-232: RP forest.  perm_dev[t*n + p] is the id
+ * at position p of tree t's leaf order; leaf_flag_dev[t*n + p] = 1 where a
+ * leaf starts.  replay (host, may be NULL) holds n_replay internal nodes as
+ * int32 sextuples (tree, level, start, size, p1_id, p2_id), e.g. the pivots
+ * the reference's std::mt19937 draws; NULL draws pivots from a counter-based
+ * hash of (seed, tree, start, size). */
+int knng_forest(knng_ctx* ctx, const int8_t* codes_dev, int64_t n, int d,
+                const int32_t* replay, int64_t n_replay, int32_t* perm_dev,
+                uint8_t* leaf_flag_dev);
+
+/* a4, src/main.cpp:220-314: initial graph ids/scores [n][k_build] from the
+ * forest, ordered by (score desc, pool position asc). */
+int knng_init_graph(knng_ctx* ctx, const int8_t* codes_dev, int64_t n, int d,
+                    const int32_t* perm_dev, const uint8_t* leaf_flag_dev, int32_t* ids_dev,
+                    int32_t* scores_dev);
+
+/* a5, src/main.cpp:324-430: one NN-Descent iteration reading ids_in/scores_in
+ * and writing ids_out/scores_out (the same pointers = in place).  The rerank
+ * set is the best k_build*rerank_mult candidates by (hamming desc, sequence
+ * position asc), visited in that order.  *updates receives the number of
+ * positions whose id changed. */
+int knng_join_iter(knng_ctx* ctx, const int8_t* codes_dev, const uint64_t* sketch_dev, int64_t n,
+                   int d, const int32_t* ids_in_dev, const int32_t* scores_in_dev,
+                   int32_t* ids_out_dev, int32_t* scores_out_dev, int64_t* updates);
+
+/* a6, src/main.cpp:446-457: knns = id + 1, dists = float(score) of the first
+ * k_eval of k_build entries, each row reversed.  id_map (may be NULL) maps
+ * internal ids to caller ids before the + 1. */
+int knng_export(const int32_t* ids_dev, const int32_t* scores_dev, int64_t n, int k_build,
+                int k_eval, const int32_t* id_map_dev, int32_t* knns_dev, float* dists_dev,
+                void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KNNG_H_ */

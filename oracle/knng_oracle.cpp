@@ -22,6 +22,7 @@
 // Exported with C linkage for ctypes (tests/, bench.py).
 #include <algorithm>
 #include <chrono>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -105,6 +106,9 @@ void oracle_default_params(oracle_params* p) {
 //   clamped = max(-128.0f, min(127.0f, scaled))   (std::min/std::max order)
 //   code    = static_cast<int8_t>(clamped)        (truncation toward zero)
 //   bit d of the sketch is set iff clamped > 0; word d/64, bit d%64.
+// Subnormal inputs are read as zero: the reference is built with -ffast-math
+// (CMakeLists.txt:6), whose start-up code enables denormals-are-zero, so a
+// subnormal x gives code 0 and sign bit 0 in the reference binary.
 // QUANT_ROUND is the optional mode that rounds half away from zero and clamps
 // to [-127, 127]; the sign bit is taken from the same clamped float.
 // sketch rows hold `words` u64; words past d/64 are written as zero.
@@ -117,7 +121,9 @@ void oracle_quantize(const float* x, int64_t n, int d, int quant_mode, int8_t* c
     uint64_t* b = sketch + i * words;
     for (int w = 0; w < words; ++w) b[w] = 0;
     for (int k = 0; k < d; ++k) {
-      float scaled = row[k] * 127.0f;
+      float v = row[k];
+      if (std::fabs(v) < FLT_MIN) v = 0.0f;
+      float scaled = v * 127.0f;
       float clamped;
       if (quant_mode == QUANT_ROUND) {
         float lo = -127.0f, hi = 127.0f;

@@ -1,0 +1,77 @@
+"""Build libknng.so (CUDA, sm_103a) and the knng_main CLI in place.
+
+    python sisap-2026-task1_gb300/build.py [--force]
+
+Each csrc/*.cu compiles to _build/<name>.o in parallel (one -gencode, sm_103a
+only), then nvcc links libknng.so next to this file; host/*.cpp link into
+knng_main against it (rpath $ORIGIN).  Targets are rebuilt only when a source
+or header is newer.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import glob
+import os
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+HOST = os.path.join(PKG, "host")
+OUT = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libknng.so")
+CLI = os.path.join(PKG, "knng_main")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+              "-diag-suppress", "550"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OUT, exist_ok=True)
+    headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    jobs = []
+    for src in sources:
+        obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
+        if force or _newer(obj, [src] + headers):
+            jobs.append([nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj])
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for r in ex.map(_run, jobs):
+            if verbose and r.stderr:
+                print(r.stderr, file=sys.stderr)
+    objs = [os.path.join(OUT, os.path.basename(s)[:-3] + ".o") for s in sources]
+    if force or jobs or _newer(LIB, objs):
+        _run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs)
+    host_srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
+    host_hdrs = glob.glob(os.path.join(HOST, "*.h"))
+    if host_srcs and (force or _newer(CLI, host_srcs + host_hdrs + [LIB])):
+        _run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include")] + host_srcs +
+             ["-o", CLI, "-L", PKG, "-lknng", "-Wl,-rpath,$ORIGIN"])
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)
+    print(LIB)

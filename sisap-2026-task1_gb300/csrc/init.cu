@@ -1,0 +1,368 @@
+// init.cu -- K3 leaf Gram blocks, K4 top-K merge into the initial graph, K6 export.
+//
+// Reference: src/main.cpp:220-314.  For each row i the reference takes the
+// union of the members of the T leaves that hold i (minus i), de-duplicates,
+// scores each by exact int8 dot, fills with xorshift32 random ids while the
+// pool holds fewer than K (state seed + i), keeps the top K by score and pads
+// with random ids of score INT32_MIN.
+//
+// Here the dots come from one Gram block per leaf (K3: every member pair of a
+// <= 64-member leaf, read once from HBM into shared memory), and a warp per
+// row merges its T leaf rows into a sorted top-K list held two entries per
+// lane (K4).  The merge keeps the K best distinct (score desc, id asc) keys,
+// which is the reference's pool order among equal scores (its pool is sorted
+// by id before the unstable partial_sort; ties are unspecified there and fixed
+// here).  Rows with fewer than K distinct candidates take the reference's
+// random-fill path exactly, one thread per row (tiny inputs only).
+#include "knng_internal.cuh"
+
+#include <algorithm>
+
+namespace knng {
+namespace {
+
+inline unsigned grid1(int64_t n, int t = 256) { return unsigned((n + t - 1) / t); }
+
+__global__ void flags_to_i32(const uint8_t* __restrict__ f, int32_t* __restrict__ o, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    o[i] = f[i];
+}
+
+// leaf_start[idx[p]] = p for every flagged position p (idx = exclusive scan of flags)
+__global__ void leaf_starts(const uint8_t* __restrict__ f, const int32_t* __restrict__ idx, int64_t n,
+                            int32_t* __restrict__ leaf_start) {
+  for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += int64_t(gridDim.x) * blockDim.x)
+    if (f[p]) leaf_start[idx[p]] = int32_t(p);
+}
+
+// per position: inverse permutation, leaf start and leaf size
+__global__ void leaf_fill(const int32_t* __restrict__ leaf_start, int64_t nleaves, int64_t total, int64_t n,
+                          const int32_t* __restrict__ perm, int32_t* __restrict__ pos, int32_t* __restrict__ leaf_lo,
+                          uint8_t* __restrict__ leaf_sz) {
+  for (int64_t l = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; l < nleaves; l += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t s = leaf_start[l];
+    const int64_t e = l + 1 < nleaves ? leaf_start[l + 1] : total;
+    const int64_t tb = (s / n) * n;
+    for (int64_t p = s; p < e; ++p) {
+      leaf_lo[p] = int32_t(s);
+      leaf_sz[p] = uint8_t(e - s);
+      pos[tb + perm[p]] = int32_t(p);
+    }
+  }
+}
+
+// K3: one block per leaf.  The leaf's <= 64 code rows are staged in shared
+// memory (row stride d + 16 bytes keeps the 8 column threads on distinct
+// banks); thread (ty, tx) owns rows 4ty..4ty+3 x columns tx + 8j and runs 128
+// dp4a per 12 shared-memory 16-byte loads.  Output: gram[p * 64 + j] = dot of
+// the members at leaf offsets (p - start) and j, for j < size.
+constexpr int kGramThreads = 128;
+
+__global__ void __launch_bounds__(kGramThreads) leaf_gram(const int8_t* __restrict__ codes, int d,
+                                                          const int32_t* __restrict__ perm,
+                                                          const int32_t* __restrict__ leaf_start,
+                                                          int64_t nleaves, int64_t total,
+                                                          int32_t* __restrict__ gram) {
+  extern __shared__ uint4 rows_s[];
+  const int stride16 = d / 16 + 1;  // in uint4
+  for (int64_t l = blockIdx.x; l < nleaves; l += gridDim.x) {
+    const int64_t s = leaf_start[l];
+    const int64_t e = l + 1 < nleaves ? leaf_start[l + 1] : total;
+    const int m = int(e - s);
+    const int nchunk = d / 16;
+    __syncthreads();
+    for (int c = threadIdx.x; c < kMaxLeaf * nchunk; c += kGramThreads) {
+      const int r = c / nchunk, cc = c % nchunk;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (r < m) v = __ldg(reinterpret_cast<const uint4*>(codes + int64_t(perm[s + r]) * d) + cc);
+      rows_s[r * stride16 + cc] = v;
+    }
+    __syncthreads();
+    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
+    if (ty * 4 >= m) continue;
+    int acc[4][8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[a][b] = 0;
+    const int jmax = (m + 7 - tx) / 8;  // columns tx + 8j < m
+    for (int c = 0; c < nchunk; ++c) {
+      uint4 A[4], B[8];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) A[a] = rows_s[(ty * 4 + a) * stride16 + c];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) B[b] = rows_s[(tx + 8 * b) * stride16 + c];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+          acc[a][b] = __dp4a(int(A[a].x), int(B[b].x), acc[a][b]);
+          acc[a][b] = __dp4a(int(A[a].y), int(B[b].y), acc[a][b]);
+          acc[a][b] = __dp4a(int(A[a].z), int(B[b].z), acc[a][b]);
+          acc[a][b] = __dp4a(int(A[a].w), int(B[b].w), acc[a][b]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int r = ty * 4 + a;
+      if (r >= m) break;
+      int32_t* out = gram + (s + r) * int64_t(kMaxLeaf);
+#pragma unroll
+      for (int b = 0; b < 8; ++b)
+        if (b < jmax) out[tx + 8 * b] = acc[a][b];
+    }
+  }
+}
+
+__device__ __forceinline__ uint64_t make_key(int32_t score, int32_t id) {
+  return (uint64_t(uint32_t(score) ^ 0x80000000u) << 32) | uint64_t(~uint32_t(id));
+}
+__device__ __forceinline__ int32_t key_score(uint64_t k) { return int32_t(uint32_t(k >> 32) ^ 0x80000000u); }
+__device__ __forceinline__ int32_t key_id(uint64_t k) { return int32_t(~uint32_t(k)); }
+
+// Insert key ck into the descending list (kA = positions 0..31, kB = 32..63),
+// length K, unless an equal key is present.  Returns the new threshold.
+__device__ __forceinline__ uint64_t list_insert(uint64_t& kA, uint64_t& kB, uint64_t ck, int K, int lane) {
+  const unsigned full = 0xffffffffu;
+  const bool present = __any_sync(full, kA == ck || kB == ck);
+  if (!present) {
+    const int pos = __popc(__ballot_sync(full, kA > ck)) + __popc(__ballot_sync(full, kB > ck));
+    const uint64_t upA = __shfl_up_sync(full, kA, 1);
+    const uint64_t a31 = __shfl_sync(full, kA, 31);
+    const uint64_t upB = __shfl_up_sync(full, kB, 1);
+    if (lane > pos) kA = upA;
+    else if (lane == pos) kA = ck;
+    const int qb = 32 + lane;
+    if (qb > pos) kB = lane == 0 ? a31 : upB;
+    else if (qb == pos) kB = ck;
+    if (lane >= K) kA = 0;
+    if (qb >= K) kB = 0;
+  }
+  return (K - 1) < 32 ? __shfl_sync(full, kA, K - 1) : __shfl_sync(full, kB, K - 33);
+}
+
+// K4: one warp per row; merge the row's T leaf Gram rows into the top-K list.
+__global__ void __launch_bounds__(256) init_merge(int64_t n, int T, int K, const int32_t* __restrict__ perm,
+                                                  const int32_t* __restrict__ pos,
+                                                  const int32_t* __restrict__ leaf_lo,
+                                                  const uint8_t* __restrict__ leaf_sz,
+                                                  const int32_t* __restrict__ gram, int32_t* __restrict__ ids,
+                                                  int32_t* __restrict__ scores, int32_t* __restrict__ fix_rows,
+                                                  int64_t* __restrict__ fix_count) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t i = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    uint64_t kA = 0, kB = 0, thr = 0;
+    for (int t = 0; t < T; ++t) {
+      const int64_t p = pos[int64_t(t) * n + i];
+      const int64_t s = leaf_lo[p];
+      const int m = leaf_sz[p];
+      const int self = int(p - s);
+      const int32_t* grow = gram + p * int64_t(kMaxLeaf);
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int j = lane + 32 * half;
+        uint64_t key = 0;
+        if (j < m && j != self) key = make_key(grow[j], perm[s + j]);
+        unsigned acc = __ballot_sync(0xffffffffu, key > thr);
+        while (acc) {
+          const int src = __ffs(acc) - 1;
+          acc &= acc - 1;
+          const uint64_t ck = __shfl_sync(0xffffffffu, key, src);
+          if (ck > thr) thr = list_insert(kA, kB, ck, K, lane);
+        }
+      }
+    }
+    const int real = __popc(__ballot_sync(0xffffffffu, kA != 0)) + __popc(__ballot_sync(0xffffffffu, kB != 0));
+    int32_t* gi = ids + i * K;
+    int32_t* gs = scores + i * K;
+    if (lane < K) {
+      gi[lane] = kA ? key_id(kA) : -1;
+      gs[lane] = kA ? key_score(kA) : kScoreMinI;
+    }
+    if (32 + lane < K) {
+      gi[32 + lane] = kB ? key_id(kB) : -1;
+      gs[32 + lane] = kB ? key_score(kB) : kScoreMinI;
+    }
+    if (real < K && lane == 0) {
+      const int64_t slot = atomicAdd(reinterpret_cast<unsigned long long*>(fix_count), 1ull);
+      fix_rows[slot] = int32_t(i);
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t xorshift32(uint32_t s) {
+  s ^= s << 13;
+  s ^= s >> 17;
+  s ^= s << 5;
+  return s;
+}
+
+__device__ int32_t dot_rows(const int8_t* a, const int8_t* b, int d) {
+  const int* pa = reinterpret_cast<const int*>(a);
+  const int* pb = reinterpret_cast<const int*>(b);
+  int s = 0;
+  for (int k = 0; k < d / 4; ++k) s = __dp4a(pa[k], pb[k], s);
+  return s;
+}
+
+// Rows whose leaves give fewer than K distinct candidates: the reference's
+// pool is (candidates by id asc) + xorshift32 fills with exact dots; sorted by
+// score (stable here), copied skipping adjacent equal ids, padded with random
+// ids of score INT32_MIN.  src/main.cpp:271-312.  One thread per row.
+__global__ void init_fixup(const int8_t* __restrict__ codes, int d, int64_t n, int K, uint32_t seed,
+                           const int32_t* __restrict__ fix_rows, int64_t nfix, int32_t* __restrict__ ids,
+                           int32_t* __restrict__ scores) {
+  const int64_t f = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (f >= nfix) return;
+  const int64_t i = fix_rows[f];
+  int32_t pid[kMaxK], psc[kMaxK];
+  int c = 0;
+  for (int k = 0; k < K; ++k)
+    if (ids[i * K + k] >= 0) {
+      pid[c] = ids[i * K + k];
+      psc[c] = scores[i * K + k];
+      ++c;
+    }
+  for (int a = 1; a < c; ++a) {  // candidates by id ascending
+    const int32_t vi = pid[a], vs = psc[a];
+    int b = a - 1;
+    while (b >= 0 && pid[b] > vi) {
+      pid[b + 1] = pid[b];
+      psc[b + 1] = psc[b];
+      --b;
+    }
+    pid[b + 1] = vi;
+    psc[b + 1] = vs;
+  }
+  uint32_t rs = seed + uint32_t(i);
+  const int8_t* vrow = codes + i * int64_t(d);
+  // xorshift32 stays at 0 from a zero state; the reference would spin there
+  // (seed + i == 0 with i == 0), so the draws are bounded.
+  int budget = 1 << 20;
+  while (c < K && --budget > 0) {
+    rs = xorshift32(rs);
+    const int64_t r = int64_t(uint64_t(rs) % uint64_t(n));
+    if (r == i) continue;
+    pid[c] = int32_t(r);
+    psc[c] = dot_rows(vrow, codes + r * int64_t(d), d);
+    ++c;
+  }
+  for (int a = 1; a < c; ++a) {  // stable by score descending
+    const int32_t vi = pid[a], vs = psc[a];
+    int b = a - 1;
+    while (b >= 0 && psc[b] < vs) {
+      pid[b + 1] = pid[b];
+      psc[b + 1] = psc[b];
+      --b;
+    }
+    pid[b + 1] = vi;
+    psc[b + 1] = vs;
+  }
+  int added = 0, last = -1;
+  for (int p = 0; p < c && added < K; ++p)
+    if (pid[p] != last) {
+      ids[i * K + added] = pid[p];
+      scores[i * K + added] = psc[p];
+      last = pid[p];
+      ++added;
+    }
+  while (added < K) {
+    rs = xorshift32(rs);
+    const int64_t r = int64_t(uint64_t(rs) % uint64_t(n));
+    if (r != i || --budget <= 0) {
+      ids[i * K + added] = int32_t(r != i ? r : (i + 1) % n);
+      scores[i * K + added] = kScoreMinI;
+      ++added;
+    }
+  }
+}
+
+__global__ void export_kernel(const int32_t* __restrict__ ids, const int32_t* __restrict__ scores, int64_t n,
+                              int K, int k_eval, const int32_t* __restrict__ id_map, int32_t* __restrict__ knns,
+                              float* __restrict__ dists) {
+  const int64_t tot = n * k_eval;
+  for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < tot; q += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t i = q / k_eval;
+    const int k = int(q % k_eval);
+    int32_t id = ids[i * K + k];
+    const int32_t sc = scores[i * K + k];
+    if (id_map) id = id_map[id];
+    const int64_t o = i * k_eval + (k_eval - 1 - k);
+    knns[o] = id + 1;
+    dists[o] = float(sc);
+  }
+}
+
+}  // namespace
+
+size_t init_bytes(int64_t n, int T, int leaf) {
+  (void)leaf;
+  const size_t tn = size_t(T) * n;
+  size_t b = tn * 4 * 3 + tn;           // pos, leaf_lo, leaf_idx, leaf_sz
+  b += tn * 4;                          // leaf starts
+  b += tn * kMaxLeaf * 4;               // gram rows
+  b += size_t(n) * 4;                   // fix rows
+  b += scan_tmp_bytes(int64_t(tn)) + 4096;
+  return b;
+}
+
+int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint32_t seed, const int32_t* perm,
+             const uint8_t* leaf_flag, int32_t* ids, int32_t* scores, const InitBufs& ib, cudaStream_t s,
+             int64_t* leaves_out, std::string* err) {
+  (void)leaf;
+  auto fail = [&](cudaError_t e, const char* what) {
+    if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+    return int(KNNG_E_CUDA);
+  };
+  cudaError_t e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t tn = int64_t(T) * n;
+  const unsigned g = unsigned(std::min<int64_t>(grid1(tn), int64_t(sms) * 32));
+  int32_t* leaf_start = ib.leaf_idx + tn;  // second half of the leaf_idx allocation
+  flags_to_i32<<<g, 256, 0, s>>>(leaf_flag, ib.leaf_idx, tn);
+  note_launch();
+  if ((e = exclusive_scan_i32(ib.leaf_idx, ib.leaf_idx, tn, ib.dev_i64, ib.scan_tmp, s))) return fail(e, "leaf scan");
+  leaf_starts<<<g, 256, 0, s>>>(leaf_flag, ib.leaf_idx, tn, leaf_start);
+  note_launch();
+  int64_t nleaves = 0;
+  if ((e = cudaMemcpyAsync(&nleaves, ib.dev_i64, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "leaf count");
+  if ((e = cudaStreamSynchronize(s))) return fail(e, "leaf table");
+  if (leaves_out) *leaves_out = nleaves;
+  leaf_fill<<<unsigned(std::min<int64_t>(grid1(nleaves), int64_t(sms) * 32)), 256, 0, s>>>(
+      leaf_start, nleaves, tn, n, perm, ib.pos, ib.leaf_lo, ib.leaf_sz);
+  note_launch();
+  const size_t smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
+  if ((e = cudaFuncSetAttribute(leaf_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))))
+    return fail(e, "gram smem");
+  leaf_gram<<<unsigned(std::min<int64_t>(nleaves, int64_t(sms) * 24)), kGramThreads, smem, s>>>(
+      codes, d, perm, leaf_start, nleaves, tn, ib.gram);
+  note_launch();
+  if ((e = cudaMemsetAsync(ib.dev_i64 + 1, 0, 8, s))) return fail(e, "fix count");
+  init_merge<<<unsigned(std::min<int64_t>((n + 7) / 8, int64_t(sms) * 16)), 256, 0, s>>>(
+      n, T, K, perm, ib.pos, ib.leaf_lo, ib.leaf_sz, ib.gram, ids, scores, ib.fix_rows, ib.dev_i64 + 1);
+  note_launch();
+  int64_t nfix = 0;
+  if ((e = cudaMemcpyAsync(&nfix, ib.dev_i64 + 1, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "fix count");
+  if ((e = cudaStreamSynchronize(s))) return fail(e, "init merge");
+  if (nfix > 0) {
+    init_fixup<<<grid1(nfix, 64), 64, 0, s>>>(codes, d, n, K, seed, ib.fix_rows, nfix, ids, scores);
+    note_launch();
+    if ((e = cudaGetLastError())) return fail(e, "init fixup");
+  }
+  return 0;
+}
+
+cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, int K, int k_eval,
+                          const int32_t* id_map, int32_t* knns, float* dists, cudaStream_t s) {
+  const int64_t tot = n * k_eval;
+  if (tot <= 0) return cudaSuccess;
+  export_kernel<<<unsigned(std::min<int64_t>(grid1(tot), 4096)), 256, 0, s>>>(ids, scores, n, K, k_eval, id_map,
+                                                                               knns, dists);
+  note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace knng

@@ -1,0 +1,240 @@
+"""Python front end of libknng.so (ctypes), the GB300 kNN-graph builder.
+
+Mirrors the reference engine's one operation -- build the all-points k-NN
+graph of /train and export knns/dists (Aftab5550/SISAP-2026-task1
+src/main.cpp:143-457) -- plus the per-stage entry points the parity tests
+drive.  Every call goes through the C ABI declared in include/knng.h; there
+is no CPU fallback: if libknng.so is missing or no GPU is visible the calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libknng.so")
+
+QUANT_TRUNC, QUANT_ROUND = 0, 1
+JOIN_JACOBI, JOIN_INPLACE = 0, 1
+ORDER_NATURAL, ORDER_LEAF = 0, 1
+
+STATUS = {0: "ok", -1: "E_ARGS", -2: "E_DIM", -3: "E_OOM", -4: "E_ADMIT", -5: "E_TIMEOUT", -6: "E_CUDA",
+          -7: "E_REPLAY", -8: "E_BUSY", -9: "E_NOTFOUND"}
+
+
+class KnngError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("k_build", C.c_int), ("k_eval", C.c_int), ("num_trees", C.c_int), ("rerank_mult", C.c_int),
+        ("leaf_size", C.c_int), ("max_iterations", C.c_int), ("early_stop_rate", C.c_float),
+        ("rate_diff_tol", C.c_float), ("quant_mode", C.c_int), ("join_mode", C.c_int),
+        ("row_order", C.c_int), ("seed", C.c_uint32), ("device", C.c_int),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("quantize_s", C.c_double), ("forest_s", C.c_double), ("init_s", C.c_double), ("join_s", C.c_double),
+        ("export_s", C.c_double), ("build_s", C.c_double), ("total_s", C.c_double), ("iterations", C.c_int),
+        ("updates", C.c_int64 * 64), ("forest_levels", C.c_int64), ("leaves", C.c_int64),
+        ("device_s", C.c_double), ("join_ms", C.c_double * 64), ("join_candidates", C.c_int64 * 64),
+        ("join_dots", C.c_int64 * 64), ("kernel_launches", C.c_int64),
+    ]
+
+    def as_dict(self):
+        arrays = ("updates", "join_ms", "join_candidates", "join_dots")
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in arrays}
+        for f in arrays:
+            d[f] = list(getattr(self, f)[: self.iterations])
+        return d
+
+
+EXPORTS = ["knng_default_params", "knng_create", "knng_destroy", "knng_build", "knng_status_string",
+           "knng_last_error", "knng_quantize", "knng_forest", "knng_init_graph", "knng_join_iter", "knng_export"]
+
+_lib = None
+
+
+def lib():
+    """Load libknng.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libknng.so not found at {LIB_PATH}: run __graft_entry__.build() first")
+        L = C.CDLL(LIB_PATH)
+        P, V, I64 = C.POINTER, C.c_void_p, C.c_int64
+        L.knng_default_params.argtypes = [P(Params)]
+        L.knng_default_params.restype = None
+        L.knng_create.argtypes = [P(V), P(Params)]
+        L.knng_destroy.argtypes = [V]
+        L.knng_destroy.restype = None
+        L.knng_build.argtypes = [V, V, I64, C.c_int, C.c_int, V, V, C.c_int, P(Stats)]
+        L.knng_status_string.argtypes = [C.c_int]
+        L.knng_status_string.restype = C.c_char_p
+        L.knng_last_error.argtypes = [V]
+        L.knng_last_error.restype = C.c_char_p
+        L.knng_quantize.argtypes = [V, I64, C.c_int, C.c_int, V, V, V]
+        L.knng_forest.argtypes = [V, V, I64, C.c_int, V, I64, V, V]
+        L.knng_init_graph.argtypes = [V, V, I64, C.c_int, V, V, V, V]
+        L.knng_join_iter.argtypes = [V, V, V, I64, C.c_int, V, V, V, V, P(I64)]
+        L.knng_export.argtypes = [V, V, I64, C.c_int, C.c_int, V, V, V, V]
+        _lib = L
+    return _lib
+
+
+def params(**kw) -> Params:
+    p = Params()
+    lib().knng_default_params(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(t):
+    """Device or host pointer of a torch tensor / numpy array (None passes through)."""
+    if t is None:
+        return None
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return C.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+
+
+class Context:
+    """A knng_ctx: device arena + CUDA stream on one GPU."""
+
+    def __init__(self, prm: Params | None = None, **kw):
+        self.prm = prm if prm is not None else params(**kw)
+        self.h = C.c_void_p()
+        self._check(lib().knng_create(C.byref(self.h), C.byref(self.prm)))
+
+    def _check(self, st):
+        if st != 0:
+            msg = lib().knng_last_error(self.h).decode() if self.h else ""
+            raise KnngError(st, msg)
+
+    def close(self):
+        if self.h:
+            lib().knng_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- whole build (src/main.cpp:179-457) --
+    def build(self, rows, knns=None, dists=None, stats: Stats | None = None):
+        """Build the graph of ``rows`` (numpy host array or torch tensor, (n, d) float32).
+
+        Outputs follow ``rows``: numpy in, numpy out; torch CUDA in, torch CUDA out.
+        Returns (knns, dists, stats).
+        """
+        st = stats or Stats()
+        n, d = rows.shape
+        k_eval = self.prm.k_eval
+        on_dev = not isinstance(rows, np.ndarray) and rows.is_cuda
+        if isinstance(rows, np.ndarray):
+            rows = np.ascontiguousarray(rows, dtype=np.float32)
+            knns = np.empty((n, k_eval), np.int32) if knns is None else knns
+            dists = np.empty((n, k_eval), np.float32) if dists is None else dists
+            out_dev = 0
+        else:
+            import torch
+
+            assert rows.dtype == torch.float32 and rows.is_contiguous()
+            out_dev = int(on_dev)
+            if knns is None:
+                knns = torch.empty((n, k_eval), dtype=torch.int32, device=rows.device if on_dev else "cpu")
+                dists = torch.empty((n, k_eval), dtype=torch.float32, device=knns.device)
+            out_dev = int(knns.is_cuda)
+        self._check(lib().knng_build(self.h, _ptr(rows), n, d, int(on_dev), _ptr(knns), _ptr(dists), out_dev,
+                                     C.byref(st)))
+        return knns, dists, st
+
+    # -- stages (torch CUDA tensors) --
+    def forest(self, codes, replay=None, perm=None, leaf_flag=None):
+        import torch
+
+        n, d = codes.shape
+        T = self.prm.num_trees
+        perm = torch.empty((T, n), dtype=torch.int32, device=codes.device) if perm is None else perm
+        leaf_flag = torch.empty((T, n), dtype=torch.uint8, device=codes.device) if leaf_flag is None else leaf_flag
+        rep = None if replay is None else np.ascontiguousarray(replay, dtype=np.int32)
+        self._check(lib().knng_forest(self.h, _ptr(codes), n, d, _ptr(rep), 0 if rep is None else len(rep),
+                                      _ptr(perm), _ptr(leaf_flag)))
+        return perm, leaf_flag
+
+    def init_graph(self, codes, perm, leaf_flag):
+        import torch
+
+        n, d = codes.shape
+        K = self.prm.k_build
+        ids = torch.empty((n, K), dtype=torch.int32, device=codes.device)
+        sc = torch.empty((n, K), dtype=torch.int32, device=codes.device)
+        self._check(lib().knng_init_graph(self.h, _ptr(codes), n, d, _ptr(perm), _ptr(leaf_flag), _ptr(ids),
+                                          _ptr(sc)))
+        return ids, sc
+
+    def join_iter(self, codes, sketch, ids_in, sc_in, ids_out=None, sc_out=None):
+        """One NN-Descent iteration; returns (ids_out, sc_out, updates).  Pass the
+        input tensors as outputs to update in place."""
+        import torch
+
+        n, d = codes.shape
+        ids_out = torch.empty_like(ids_in) if ids_out is None else ids_out
+        sc_out = torch.empty_like(sc_in) if sc_out is None else sc_out
+        up = C.c_int64(0)
+        self._check(lib().knng_join_iter(self.h, _ptr(codes), _ptr(sketch), n, d, _ptr(ids_in), _ptr(sc_in),
+                                         _ptr(ids_out), _ptr(sc_out), C.byref(up)))
+        return ids_out, sc_out, up.value
+
+
+def quantize(x, quant_mode=QUANT_TRUNC, stream=None):
+    """K1 on a CUDA float32 tensor: returns (codes int8 (n, d), sketch int64 (n, d/64))."""
+    import torch
+
+    n, d = x.shape
+    codes = torch.empty((n, d), dtype=torch.int8, device=x.device)
+    sk = torch.empty((n, d // 64), dtype=torch.int64, device=x.device)
+    st = lib().knng_quantize(_ptr(x), n, d, quant_mode, _ptr(codes), _ptr(sk), _stream_ptr(stream))
+    if st != 0:
+        raise KnngError(st, "knng_quantize")
+    torch.cuda.synchronize(x.device)
+    return codes, sk
+
+
+def export(ids, scores, k_eval=15, id_map=None, stream=None):
+    import torch
+
+    n, K = ids.shape
+    knns = torch.empty((n, k_eval), dtype=torch.int32, device=ids.device)
+    dists = torch.empty((n, k_eval), dtype=torch.float32, device=ids.device)
+    st = lib().knng_export(_ptr(ids), _ptr(scores), n, K, k_eval, _ptr(id_map), _ptr(knns), _ptr(dists),
+                           _stream_ptr(stream))
+    if st != 0:
+        raise KnngError(st, "knng_export")
+    torch.cuda.synchronize(ids.device)
+    return knns, dists

@@ -37,9 +37,11 @@ CASES = {
 
 # Values at the quantiser's corners (src/main.cpp:184-190): sub-code positives
 # (code 0, sign bit 1), sub-code negatives, exact +-1, beyond the clamp on both
-# sides, signed zeros and values that truncate rather than round.
+# sides, signed zeros, values that truncate rather than round, and subnormals
+# (read as zero by the reference's -ffast-math build).
 EDGE_VALUES = np.array([0.5 / 127, -0.5 / 127, 1.0, -1.0, 1.02, -1.5, 127.4 / 127, -128.6 / 127,
-                        0.0, -0.0, 2.9 / 127, -2.9 / 127, 126.99 / 127, -127.99 / 127, 3.0, -3.0],
+                        0.0, -0.0, 2.9 / 127, -2.9 / 127, 126.99 / 127, -127.99 / 127, 3.0, -3.0,
+                        1e-40, -1e-40],
                        dtype=np.float32)
 
 

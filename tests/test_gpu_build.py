@@ -1,0 +1,149 @@
+"""Whole builds through knng_build (C ABI), judged as the reference's output is.
+
+The graph is nondeterministic in the reference (threads race, nth_element and
+partial_sort ties), so builds are compared by recall@15 against exact float64
+brute force: the GPU build must land no more than 0.5 points below the
+reference binary's recall on the same input (fixtures in tests/golden).  At
+larger sizes size-independent properties are checked instead: each exported
+row is a sorted list of distinct ids != self whose dists are the exact int8
+inner products.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import synth
+
+pytestmark = pytest.mark.gpu
+RECALL_TOL = 0.005
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def knng_mod():
+    import torch
+
+    assert torch.cuda.is_available(), "the gpu tests need a CUDA device"
+    import knng
+
+    knng.lib()
+    return knng
+
+
+def _golden(name):
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(HERE, "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    x = mg.make_input(*mg.CASES[name])
+    return x, np.load(os.path.join(HERE, "golden", name + ".npz"))
+
+
+def _check_export(x, knns, dists):
+    n = x.shape[0]
+    codes, _ = oracle.quantize(x)
+    ids = knns.astype(np.int64) - 1
+    assert ids.min() >= 0 and ids.max() < n
+    assert not np.any(ids == np.arange(n)[:, None])
+    assert np.all(np.diff(dists, axis=1) >= 0)  # worst -> best
+    sample = np.arange(0, n, max(1, n // 500))
+    exact = np.einsum("id,ikd->ik", codes[sample].astype(np.int32), codes[ids[sample]].astype(np.int32))
+    np.testing.assert_array_equal(dists[sample], exact.astype(np.float32))
+    for row in ids[sample]:
+        assert len(np.unique(row)) == len(row)
+
+
+@pytest.mark.parametrize("name", ["mix_n2000_d1024", "mix_n6000_d1024_c600", "mix_n3000_d384", "mix_n2500_d768"])
+@pytest.mark.parametrize("join", ["jacobi", "inplace"])
+def test_build_recall_vs_reference(knng_mod, name, join):
+    knng = knng_mod
+    x, g = _golden(name)
+    gt = synth.exact_knn(x, 15)
+    ref_recall = synth.recall_at_k(g["knns"], gt)
+    mode = knng.JOIN_JACOBI if join == "jacobi" else knng.JOIN_INPLACE
+    with knng.Context(join_mode=mode) as ctx:
+        knns, dists, st = ctx.build(x)
+    rec = synth.recall_at_k(knns, gt)
+    assert rec >= ref_recall - RECALL_TOL, (rec, ref_recall)
+    _check_export(x, knns, dists)
+
+
+def test_build_tiny_inputs(knng_mod):
+    knng = knng_mod
+    for name in ("tiny_n2_d1024", "tiny_n40_d1024"):
+        x, g = _golden(name)
+        with knng.Context() as ctx:
+            knns, dists, st = ctx.build(x)
+        # the score vectors are those of the reference (ties aside, ids may differ)
+        np.testing.assert_array_equal(dists, g["dists"])
+
+
+def test_build_is_deterministic_and_io_independent(knng_mod):
+    import torch
+
+    knng = knng_mod
+    x = synth.mixture(20000, 1024, 200, seed=21)
+    with knng.Context() as ctx:
+        k1, d1, _ = ctx.build(x)
+        k2, d2, _ = ctx.build(x)
+        xd = torch.from_numpy(x).cuda()
+        k3, d3, _ = ctx.build(xd)
+    np.testing.assert_array_equal(k1, k2)
+    np.testing.assert_array_equal(d1, d2)
+    np.testing.assert_array_equal(k1, k3.cpu().numpy())
+    np.testing.assert_array_equal(d1, d3.cpu().numpy())
+
+
+def test_build_natural_and_leaf_order_agree(knng_mod):
+    knng = knng_mod
+    x = synth.mixture(8000, 768, 80, seed=22)
+    with knng.Context(row_order=knng.ORDER_NATURAL) as a, knng.Context(row_order=knng.ORDER_LEAF) as b:
+        ka, da, _ = a.build(x)
+        kb, db, _ = b.build(x)
+    np.testing.assert_array_equal(ka, kb)  # the Jacobi join does not depend on the row order
+    np.testing.assert_array_equal(da, db)
+
+
+def test_build_rejects_bad_shapes(knng_mod):
+    knng = knng_mod
+    with knng.Context() as ctx:
+        with pytest.raises(knng.KnngError) as e1:
+            ctx.build(np.zeros((1, 1024), np.float32))
+        assert e1.value.status == -1
+        with pytest.raises(knng.KnngError) as e2:
+            ctx.build(np.zeros((100, 100), np.float32))
+        assert e2.value.status == -2
+    with pytest.raises(knng.KnngError):
+        knng.Context(k_build=65)
+
+
+def test_build_one_million_properties(knng_mod):
+    """1M x 1024 (the single-build configuration): properties on sampled rows and
+    recall on 1,000 rows against exact brute force computed on the GPU."""
+    import torch
+
+    knng = knng_mod
+    n, d = 1_000_000, 1024
+    x = synth.mixture_torch(n, d, 10_000, seed=1001)
+    with knng.Context() as ctx:
+        knns, dists, st = ctx.build(x)
+    assert st.iterations >= 1
+    kh, dh = knns.cpu().numpy(), dists.cpu().numpy()
+    ids = kh.astype(np.int64) - 1
+    assert ids.min() >= 0 and ids.max() < n and not np.any(ids == np.arange(n)[:, None])
+    assert np.all(np.diff(dh, axis=1) >= 0)
+    rows = torch.randperm(n, generator=torch.Generator().manual_seed(7))[:1000].numpy()
+    codes, _ = knng.quantize(x[torch.from_numpy(rows).cuda()])
+    nb = torch.from_numpy(ids[rows]).cuda()
+    qc = knng.quantize(x)[0]
+    exact = torch.einsum("id,ikd->ik", codes.int().double(), qc[nb].int().double()).cpu().numpy()
+    np.testing.assert_array_equal(dh[rows], exact.astype(np.float32))
+    xs = x[torch.from_numpy(rows).cuda()].double()
+    sims = xs @ x.double().T
+    sims[torch.arange(len(rows)), torch.from_numpy(rows).cuda()] = -np.inf
+    gt = sims.topk(15, dim=1).indices.cpu().numpy()
+    rec = synth.recall_at_k(kh, gt, rows=rows)
+    assert rec > 0.5, rec
