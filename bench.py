@@ -151,8 +151,8 @@ def recall_sample(x, knns, rows=10_000, seed=7):
     g = torch.Generator().manual_seed(seed)
     idx = torch.randperm(n, generator=g)[: min(rows, n)].to(x.device)
     gt = []
-    for s in range(0, len(idx), 1000):
-        q = idx[s:s + 1000]
+    for s in range(0, len(idx), 500):
+        q = idx[s:s + 500]
         sims = x[q] @ x.T  # fp32 pass, then fp64 rescoring of the best 64
         sims[torch.arange(len(q), device=x.device), q] = -float("inf")
         cand = sims.topk(64, dim=1).indices

@@ -101,7 +101,9 @@ void knng_destroy(knng_ctx* ctx);
  *             (src/main.cpp:452, 455).
  * dists     : n * k_eval float32 int8 inner products, same order (:453, 456).
  * out_on_device selects whether knns/dists are device pointers.
- * stats may be NULL. */
+ * stats may be NULL.  The call works on the context's own non-blocking
+ * stream and returns after the results are complete; device input must be
+ * fully written before the call (it does not wait for other streams). */
 int knng_build(knng_ctx* ctx, const void* rows, int64_t n, int d, int rows_on_device,
                int32_t* knns, float* dists, int out_on_device, knng_stats* stats);
 

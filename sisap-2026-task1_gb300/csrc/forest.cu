@@ -272,6 +272,20 @@ __global__ void children_emit(NodeArr nd, int cnt, int leaf, const int32_t* tile
 
 inline unsigned grid1(int64_t n, int t = 256) { return unsigned((n + t - 1) / t); }
 
+// Depth valve.  When pivots cannot separate a node (every member has the same
+// code, so d1 == d2 sends all but p1 right) each level peels off one member and
+// the depth grows with n; the reference recurses to that depth too.  Past
+// kMaxLevels the remaining active nodes are cut into consecutive leaf_size
+// leaves.  Real data stays far below (about 40 levels at 1M rows).
+constexpr int kMaxLevels = 2048;
+
+__global__ void chunk_leaves(NodeArr nd, int cnt, int leaf, uint8_t* leaf_flag) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= cnt) return;
+  const int64_t s = nd.start[k], e = s + nd.size[k];
+  for (int64_t p = s; p < e; p += leaf) leaf_flag[p] = 1;
+}
+
 }  // namespace
 
 size_t forest_bytes(int64_t n, int T, int leaf, int64_t* max_nodes, int64_t* max_tiles) {
@@ -338,6 +352,11 @@ int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t 
   int level = 0;
   int64_t host_i64[2];
   while (cnt > 0) {
+    if (level >= kMaxLevels) {
+      chunk_leaves<<<grid1(cnt), 256, 0, s>>>(cur, int(cnt), leaf, leaf_flag);
+      note_launch();
+      break;
+    }
     const int32_t* rep_dev = nullptr;
     if (replay_host) {
       if (size_t(level) + 1 >= lvl_off.size() || lvl_off[level + 1] - lvl_off[level] != cnt) {

@@ -109,6 +109,17 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
+def _ready(*tensors):
+    """The library works on its own non-blocking stream, which does not wait for
+    torch's streams: finish pending torch work on the tensors' device first."""
+    for t in tensors:
+        if t is not None and not isinstance(t, np.ndarray) and t.is_cuda:
+            import torch
+
+            torch.cuda.synchronize(t.device)
+            return
+
+
 def _stream_ptr(stream):
     if stream is None:
         return None
@@ -170,6 +181,7 @@ class Context:
                 knns = torch.empty((n, k_eval), dtype=torch.int32, device=rows.device if on_dev else "cpu")
                 dists = torch.empty((n, k_eval), dtype=torch.float32, device=knns.device)
             out_dev = int(knns.is_cuda)
+        _ready(rows, knns)
         self._check(lib().knng_build(self.h, _ptr(rows), n, d, int(on_dev), _ptr(knns), _ptr(dists), out_dev,
                                      C.byref(st)))
         return knns, dists, st
@@ -183,6 +195,7 @@ class Context:
         perm = torch.empty((T, n), dtype=torch.int32, device=codes.device) if perm is None else perm
         leaf_flag = torch.empty((T, n), dtype=torch.uint8, device=codes.device) if leaf_flag is None else leaf_flag
         rep = None if replay is None else np.ascontiguousarray(replay, dtype=np.int32)
+        _ready(codes)
         self._check(lib().knng_forest(self.h, _ptr(codes), n, d, _ptr(rep), 0 if rep is None else len(rep),
                                       _ptr(perm), _ptr(leaf_flag)))
         return perm, leaf_flag
@@ -194,6 +207,7 @@ class Context:
         K = self.prm.k_build
         ids = torch.empty((n, K), dtype=torch.int32, device=codes.device)
         sc = torch.empty((n, K), dtype=torch.int32, device=codes.device)
+        _ready(codes)
         self._check(lib().knng_init_graph(self.h, _ptr(codes), n, d, _ptr(perm), _ptr(leaf_flag), _ptr(ids),
                                           _ptr(sc)))
         return ids, sc
@@ -207,6 +221,7 @@ class Context:
         ids_out = torch.empty_like(ids_in) if ids_out is None else ids_out
         sc_out = torch.empty_like(sc_in) if sc_out is None else sc_out
         up = C.c_int64(0)
+        _ready(codes)
         self._check(lib().knng_join_iter(self.h, _ptr(codes), _ptr(sketch), n, d, _ptr(ids_in), _ptr(sc_in),
                                          _ptr(ids_out), _ptr(sc_out), C.byref(up)))
         return ids_out, sc_out, up.value
@@ -219,6 +234,8 @@ def quantize(x, quant_mode=QUANT_TRUNC, stream=None):
     n, d = x.shape
     codes = torch.empty((n, d), dtype=torch.int8, device=x.device)
     sk = torch.empty((n, d // 64), dtype=torch.int64, device=x.device)
+    if stream is not None:
+        _ready(x)
     st = lib().knng_quantize(_ptr(x), n, d, quant_mode, _ptr(codes), _ptr(sk), _stream_ptr(stream))
     if st != 0:
         raise KnngError(st, "knng_quantize")
