@@ -132,7 +132,9 @@ def test_init_graph_bit_exact(torch_dev, n, d, c, leaf, trees):
                                  torch.from_numpy(lf_ref).to(dev))
     np.testing.assert_array_equal(sc.cpu().numpy(), sc_ref)
     np.testing.assert_array_equal(ids.cpu().numpy(), ids_ref)
-    # the reference's own (unstable) tie order gives the same score vectors
+    if n < 1000:
+        return  # random fills: adjacent-duplicate removal depends on the sort's tie order
+    # without random fills the reference's own (unstable) tie order gives the same score vectors
     _, sc_tie = oracle.init_graph(codes_ref, perm_ref, lf_ref, oracle.params(threads=1, leaf_size=leaf,
                                                                               num_trees=trees))
     np.testing.assert_array_equal(sc.cpu().numpy(), sc_tie)
