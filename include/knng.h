@@ -37,7 +37,8 @@ typedef enum knng_status {
   KNNG_E_CUDA = -6,    /* CUDA runtime error (message: knng_last_error) */
   KNNG_E_REPLAY = -7,  /* replay pivot table does not match the forest */
   KNNG_E_BUSY = -8,    /* ticket not finished yet (knng_poll) */
-  KNNG_E_NOTFOUND = -9 /* unknown ticket */
+  KNNG_E_NOTFOUND = -9, /* unknown ticket */
+  KNNG_E_SCRATCH = -10  /* input too large for knng_init_graph_noalloc's fixed scratch */
 } knng_status;
 
 enum { KNNG_QUANT_TRUNC = 0, KNNG_QUANT_ROUND = 1 };
@@ -149,6 +150,27 @@ int knng_join_iter(knng_ctx* ctx, const int8_t* codes_dev, const uint64_t* sketc
 int knng_export(const int32_t* ids_dev, const int32_t* scores_dev, int64_t n, int k_build,
                 int k_eval, const int32_t* id_map_dev, int32_t* knns_dev, float* dists_dev,
                 void* stream);
+
+/* No counterpart in the reference (it allocates with std::vector on the host
+ * and has no device code).  The initial-graph stage of knng_init_graph for
+ * callers that may not allocate device memory: processes whose GPU memory is
+ * owned by another allocator (a framework's caching pool, a database's device
+ * memory manager, a plugin host), where a raw cudaMalloc would escape or
+ * fragment that pool and cudaFree would synchronise the whole device.  The
+ * caller passes inputs and outputs as in knng_init_graph, plus the parameters
+ * a context would hold; the stage's scratch is one fixed 64 MiB device array
+ * inside libknng.so (held by every GPU that loads the library until exit), so
+ * num_trees * n is limited to about 240,000 (about 15,000 rows with 16 trees);
+ * larger inputs return KNNG_E_SCRATCH before any device work.  It calls no
+ * cudaMalloc, cudaFree or allocating library routine.  The first call on each
+ * device (with that device current) resolves the array's device address; make
+ * it before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race and must be serialised.  Returns after `stream` has finished
+ * the stage (NULL = the legacy default stream). */
+int knng_init_graph_noalloc(const int8_t* codes_dev, int64_t n, int d, int num_trees, int leaf_size,
+                            int k_build, uint32_t seed, const int32_t* perm_dev,
+                            const uint8_t* leaf_flag_dev, int32_t* ids_dev, int32_t* scores_dev,
+                            void* stream);
 
 #ifdef __cplusplus
 }

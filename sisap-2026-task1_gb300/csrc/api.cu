@@ -223,6 +223,7 @@ const char* knng_status_string(int s) {
     case KNNG_E_REPLAY: return "replay pivot table mismatch";
     case KNNG_E_BUSY: return "job not finished";
     case KNNG_E_NOTFOUND: return "unknown ticket";
+    case KNNG_E_SCRATCH: return "input exceeds the fixed no-allocation scratch";
     default: return "unknown status";
   }
 }

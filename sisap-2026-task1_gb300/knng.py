@@ -22,7 +22,7 @@ JOIN_JACOBI, JOIN_INPLACE = 0, 1
 ORDER_NATURAL, ORDER_LEAF = 0, 1
 
 STATUS = {0: "ok", -1: "E_ARGS", -2: "E_DIM", -3: "E_OOM", -4: "E_ADMIT", -5: "E_TIMEOUT", -6: "E_CUDA",
-          -7: "E_REPLAY", -8: "E_BUSY", -9: "E_NOTFOUND"}
+          -7: "E_REPLAY", -8: "E_BUSY", -9: "E_NOTFOUND", -10: "E_SCRATCH"}
 
 
 class KnngError(RuntimeError):
@@ -58,7 +58,8 @@ class Stats(C.Structure):
 
 
 EXPORTS = ["knng_default_params", "knng_create", "knng_destroy", "knng_build", "knng_status_string",
-           "knng_last_error", "knng_quantize", "knng_forest", "knng_init_graph", "knng_join_iter", "knng_export"]
+           "knng_last_error", "knng_quantize", "knng_forest", "knng_init_graph", "knng_join_iter", "knng_export",
+           "knng_init_graph_noalloc"]
 
 _lib = None
 
@@ -86,6 +87,7 @@ def lib():
         L.knng_init_graph.argtypes = [V, V, I64, C.c_int, V, V, V, V]
         L.knng_join_iter.argtypes = [V, V, V, I64, C.c_int, V, V, V, V, P(I64)]
         L.knng_export.argtypes = [V, V, I64, C.c_int, C.c_int, V, V, V, V]
+        L.knng_init_graph_noalloc.argtypes = [V, I64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32, V, V, V, V, V]
         _lib = L
     return _lib
 
@@ -255,3 +257,22 @@ def export(ids, scores, k_eval=15, id_map=None, stream=None):
         raise KnngError(st, "knng_export")
     torch.cuda.synchronize(ids.device)
     return knns, dists
+
+
+def init_graph_noalloc(codes, perm, leaf_flag, num_trees=16, leaf_size=64, k_build=50, seed=1337, ids=None,
+                       scores=None, stream=None):
+    """knng_init_graph_noalloc: the initial-graph stage with the library's fixed
+    64 MiB device scratch instead of any allocation by the library.  For callers
+    whose device memory is owned by another allocator; outputs may be passed in
+    (preallocated from that allocator).  Returns (ids, scores)."""
+    import torch
+
+    n, d = codes.shape
+    ids = torch.empty((n, k_build), dtype=torch.int32, device=codes.device) if ids is None else ids
+    scores = torch.empty((n, k_build), dtype=torch.int32, device=codes.device) if scores is None else scores
+    _ready(codes, perm, leaf_flag)
+    st = lib().knng_init_graph_noalloc(_ptr(codes), n, d, num_trees, leaf_size, k_build, seed, _ptr(perm),
+                                       _ptr(leaf_flag), _ptr(ids), _ptr(scores), _stream_ptr(stream))
+    if st != 0:
+        raise KnngError(st, "knng_init_graph_noalloc")
+    return ids, scores
