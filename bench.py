@@ -34,6 +34,7 @@ CONFIGS = {
     # name: (n, d, centres, description)
     "full": (6_350_000, 1024, 50_000, "full-scale single build 6.35M x 1024, 50k centres"),
     "1m": (1_000_000, 1024, 10_000, "single build 1M x 1024, 10k centres"),
+    "300k": (300_000, 1024, 3_000, "profiling case 300k x 1024, 3k centres (codes+sketches 0.34 GB > L2)"),
     "small": (100_000, 1024, 1_000, "plain small 100k x 1024, 1k centres"),
 }
 CPU_SAMPLE = (100_000, 1024, 1_000)  # bounded CPU sample (the 100k small config), ~10-30 s of CPU work
