@@ -21,18 +21,33 @@
 // (h desc, j asc) and replays the reference's insertion loop over them in one
 // warp, with the pool held two entries per lane.
 //
-// Stages per row (shared memory, K = 50, R = 400, d = 1024: ~27 KB):
-//   A  own list, sketch, code row; clear the h histogram
-//   B  gather the K*K two-hop ids (K rows of K ids, contiguous per row)
-//   C  Hamming: 8 lanes per candidate, one 16-byte sketch chunk per lane
-//      (128-byte rows = one coalesced line per candidate), warp __popc
-//   D  threshold h_t from the histogram (warp scan over 1025 bins)
-//   E  selection: all h > h_t plus the first R - count(h > h_t) with h == h_t
-//      in j order (one block scan of per-thread tie counts)
-//   F  drop ids in the starting pool; dp4a dots, 8 lanes per candidate
-//   G  rank-sort the promising candidates by (h desc, j asc)
+// Duplicates: only ~25-30 % of the K*K two-hop candidates of a row are
+// distinct ids, so each row first inserts them into a shared-memory hash table
+// (open addressing, keys = ids).  Every occurrence of an id has the same h, so
+// h and the dot are computed once per distinct id.  Among the occurrences of
+// one id only the first in visit order can change the list (a later one finds
+// the id in the list, or scores <= the threshold that evicted or rejected it),
+// and when one occurrence is selected so is the first (ties at the cut are
+// taken in j order), so the visit key of a distinct id is (h, first j).
+//
+// Stages per row (shared memory, K = 50, R = 400, d = 1024: ~55 KB):
+//   A  own list, sketch, code row; clear table and histogram; insert the
+//      starting list's ids with a real score, flagged (bit 31 of the key)
+//   B  two-hop ids: warp per neighbour row (K contiguous ids), insert each,
+//      record its slot per j and the first j per slot (atomicMin)
+//   C  compact the distinct candidate slots; Hamming once per distinct id:
+//      8 lanes per candidate, one 16-byte sketch chunk per lane (128-byte
+//      rows = one line per candidate), warp __popc
+//   D  histogram of h over all occurrences, threshold h_t (warp scan)
+//   E  selection: every occurrence with h > h_t plus the first
+//      R - count(h > h_t) occurrences with h == h_t in j order (one block scan
+//      of per-thread tie counts); marks the selected slots
+//   F  selected ids not flagged as starting-list members: dp4a dots, 8 lanes
+//      per candidate; keep those above the starting pool[K-1].score
+//   G  rank-sort the survivors by (h desc, first j asc)
 //   H  sequential insertion + write-back + update count (warp 0)
-// HBM-bound: per row K*4*K (ids) + K*K*d/8 (sketches) + <= R*d (code rows).
+// Per row HBM/L2 bytes: K*8 (own list) + K*K*4 (two-hop ids) + d + d/8 (own
+// row, sketch) + U*d/8 (U distinct candidates) + r*d (r reranked rows).
 #include "knng_internal.cuh"
 
 #include <algorithm>
@@ -44,12 +59,16 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kGroups = kThreads / 8;  // 8-lane groups per CTA
 constexpr int kHBins = 1025;
+constexpr int32_t kEmpty = 0x7fffffff;     // never a valid id (num_trees * n < 2^31)
+constexpr uint32_t kPoolFlag = 0x80000000u; // key bit: id is in the starting list with a real score
+constexpr uint32_t kFirstMask = 0x1fffu;    // meta bits 0..12: first j (8191 = none)
+constexpr uint32_t kSelFlag = 0x80000000u;  // meta bit 31: selected for rerank
 
 struct JoinSmem {
-  int K, R, KK, d, W;
+  int K, R, KK, d, W, HT;
   size_t bytes;
-  size_t o_cand_id, o_cand_h, o_hist, o_sel, o_need, o_pkey, o_pid, o_pdot, o_order, o_pool_id, o_pool_sc,
-      o_code, o_sk;
+  size_t o_code, o_sk, o_slot, o_key, o_meta, o_hist, o_ulist, o_need, o_pkey, o_pid, o_pdot, o_order, o_pool_id,
+      o_pool_sc;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -61,13 +80,16 @@ __host__ __device__ inline JoinSmem join_smem(int K, int R, int d) {
   s.KK = K * K;
   s.d = d;
   s.W = d / 64;
+  s.HT = 1024;
+  while (s.HT < (3 * (s.KK + K)) / 2) s.HT <<= 1;  // load factor <= 2/3
   size_t o = 0;
   s.o_code = o;    o = align16(o + size_t(d));
   s.o_sk = o;      o = align16(o + size_t(s.W) * 8);
-  s.o_cand_id = o; o = align16(o + size_t(s.KK) * 4);
-  s.o_cand_h = o;  o = align16(o + size_t(s.KK) * 2);
+  s.o_slot = o;    o = align16(o + size_t(s.KK) * 2);
+  s.o_key = o;     o = align16(o + size_t(s.HT) * 4);
+  s.o_meta = o;    o = align16(o + size_t(s.HT) * 4);
   s.o_hist = o;    o = align16(o + size_t(kHBins) * 4);
-  s.o_sel = o;     o = align16(o + size_t(R) * 2);
+  s.o_ulist = o;   o = align16(o + size_t(s.KK) * 2);
   s.o_need = o;    o = align16(o + size_t(R) * 2);
   s.o_pkey = o;    o = align16(o + size_t(R) * 4);
   s.o_pid = o;     o = align16(o + size_t(R) * 4);
@@ -90,6 +112,27 @@ __device__ __forceinline__ int dot_u4(uint4 a, uint4 b, int acc) {
   return __dp4a(int(a.w), int(b.w), acc);
 }
 
+__device__ __forceinline__ uint32_t hash_slot(int32_t id, uint32_t mask) {
+  return (uint32_t(id) * 2654435761u >> 7) & mask;
+}
+
+// Find or insert id (flagged keys match by their low 31 bits).  The table
+// always has free slots (load <= 2/3), so the probe ends; the bound is a guard.
+__device__ __forceinline__ int table_insert(int32_t* key, uint32_t mask, int32_t id, uint32_t flag) {
+  uint32_t s = hash_slot(id, mask);
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    int32_t k = key[s];
+    if (k == kEmpty) {
+      const int32_t prev = atomicCAS(&key[s], kEmpty, int32_t(uint32_t(id) | flag));
+      if (prev == kEmpty) return int(s);
+      k = prev;
+    }
+    if ((uint32_t(k) & 0x7fffffffu) == uint32_t(id)) return int(s);
+    s = (s + 1) & mask;
+  }
+  return -1;
+}
+
 __global__ void __launch_bounds__(kThreads, 4) join_kernel(
     const int8_t* __restrict__ codes, const uint64_t* __restrict__ sketch, int64_t n, int d, int K, int R,
     const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out, int32_t* scores_out,
@@ -98,22 +141,24 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
   const JoinSmem L = join_smem(K, R, d);
   uint4* my_code = reinterpret_cast<uint4*>(smem + L.o_code);
   uint4* my_sk = reinterpret_cast<uint4*>(smem + L.o_sk);
-  int32_t* cand_id = reinterpret_cast<int32_t*>(smem + L.o_cand_id);
-  uint16_t* cand_h = reinterpret_cast<uint16_t*>(smem + L.o_cand_h);
+  int16_t* cand_slot = reinterpret_cast<int16_t*>(smem + L.o_slot);
+  int32_t* key = reinterpret_cast<int32_t*>(smem + L.o_key);
+  uint32_t* meta = reinterpret_cast<uint32_t*>(smem + L.o_meta);
   uint32_t* hist = reinterpret_cast<uint32_t*>(smem + L.o_hist);
-  uint16_t* sel = reinterpret_cast<uint16_t*>(smem + L.o_sel);
-  uint16_t* need = reinterpret_cast<uint16_t*>(smem + L.o_need);
+  int16_t* ulist = reinterpret_cast<int16_t*>(smem + L.o_ulist);
+  int16_t* need = reinterpret_cast<int16_t*>(smem + L.o_need);
   uint32_t* pkey = reinterpret_cast<uint32_t*>(smem + L.o_pkey);
   int32_t* pid = reinterpret_cast<int32_t*>(smem + L.o_pid);
   int32_t* pdot = reinterpret_cast<int32_t*>(smem + L.o_pdot);
   uint16_t* order = reinterpret_cast<uint16_t*>(smem + L.o_order);
   int32_t* pool_id = reinterpret_cast<int32_t*>(smem + L.o_pool_id);
   int32_t* pool_sc = reinterpret_cast<int32_t*>(smem + L.o_pool_sc);
-  __shared__ int s_cnt, s_ht, s_gt, s_nsel, s_nneed, s_nprom;
+  __shared__ int s_cnt, s_ht, s_gt, s_nu, s_nneed, s_nprom;
   __shared__ int32_t s_wsum[kWarps];
 
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, sub = lane & 7;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, sub = lane & 7, slot8 = lane >> 3;
   const int KK = L.KK, W = L.W, nchunk = d / 16, sk_chunks = W / 2;
+  const uint32_t mask = uint32_t(L.HT - 1);
   const bool inplace = ids_out == ids_in;
   unsigned long long my_updates = 0, my_cands = 0, my_dots = 0;
 
@@ -127,64 +172,88 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
     for (int c = tid; c < nchunk; c += kThreads) my_code[c] = reinterpret_cast<const uint4*>(codes + i * d)[c];
     for (int c = tid; c < sk_chunks; c += kThreads) my_sk[c] = reinterpret_cast<const uint4*>(sketch + i * W)[c];
     for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;
+    for (int t = tid; t < L.HT; t += kThreads) {
+      key[t] = kEmpty;
+      meta[t] = kFirstMask;
+    }
     if (tid == 0) {
       s_cnt = 0;
-      s_nsel = 0;
+      s_nu = 0;
       s_nneed = 0;
       s_nprom = 0;
     }
     __syncthreads();
-    // ---- B
-    for (int j = tid; j < KK; j += kThreads) {
-      const int k = j / K, k2 = j - k * K;
-      const int32_t n1 = pool_id[k];
-      const int32_t n2 = (n1 >= 0 && n1 < n) ? ids_in[int64_t(n1) * K + k2] : -1;
-      cand_id[j] = (n2 == i || n2 < 0 || n2 >= n) ? -1 : n2;
+    for (int k = tid; k < K; k += kThreads) {
+      const int32_t id = pool_id[k];
+      if (pool_sc[k] != kScoreMinI && id >= 0 && id < n) table_insert(key, mask, id, kPoolFlag);
     }
     __syncthreads();
-    // ---- C  (groups of 8 lanes; 4 candidates in flight per group)
+    // ---- B  (warp per neighbour row; no division)
+    int local_cnt = 0;
+    for (int k = warp; k < K; k += kWarps) {
+      const int32_t n1 = pool_id[k];
+      const bool ok = n1 >= 0 && n1 < n;
+      for (int k2 = lane; k2 < K; k2 += 32) {
+        const int j = k * K + k2;
+        int32_t n2 = ok ? ids_in[int64_t(n1) * K + k2] : -1;
+        int sl = -1;
+        if (n2 >= 0 && n2 < n && n2 != i) sl = table_insert(key, mask, n2, 0u);
+        cand_slot[j] = int16_t(sl);
+        if (sl >= 0) {
+          atomicMin(&meta[sl], uint32_t(j));
+          ++local_cnt;
+        }
+      }
+    }
+    if (local_cnt) atomicAdd(&s_cnt, local_cnt);
+    __syncthreads();
+    // ---- C0  distinct candidate slots (touched by an occurrence)
+    for (int t = tid; t < L.HT; t += kThreads) {
+      const bool touched = (meta[t] & kFirstMask) != kFirstMask;
+      const unsigned bal = __ballot_sync(0xffffffffu, touched);
+      int base = 0;
+      if (lane == 0 && bal) base = atomicAdd(&s_nu, __popc(bal));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (touched) ulist[base + __popc(bal & ((1u << lane) - 1u))] = int16_t(t);
+    }
+    __syncthreads();
+    // ---- C  Hamming once per distinct id (groups of 8 lanes, 4 in flight)
+    const int nu = s_nu;
     {
       const uint4 mine = sub < sk_chunks ? my_sk[sub] : make_uint4(0, 0, 0, 0);
-      int local_cnt = 0;
-      const int slot = lane >> 3;
-      // the loop bound is warp-uniform so every lane reaches the shuffles
-      for (int wbase = warp * 4; wbase < KK; wbase += 4 * kGroups) {
-        const int base = wbase + slot;
+      for (int wbase = warp * 4; wbase < nu; wbase += 4 * kGroups) {
+        const int base = wbase + slot8;
         uint4 v[4];
-        int cj[4];
+        int sl[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const int j = base + u * kGroups;
-          cj[u] = j < KK ? cand_id[j] : -1;
+          const int q = base + u * kGroups;
+          sl[u] = q < nu ? int(ulist[q]) : -1;
           v[u] = make_uint4(0, 0, 0, 0);
-          if (cj[u] >= 0 && sub < sk_chunks)
-            v[u] = __ldg(reinterpret_cast<const uint4*>(sketch + int64_t(cj[u]) * W) + sub);
+          if (sl[u] >= 0 && sub < sk_chunks) {
+            const int32_t id = int32_t(uint32_t(key[sl[u]]) & 0x7fffffffu);
+            v[u] = __ldg(reinterpret_cast<const uint4*>(sketch + int64_t(id) * W) + sub);
+          }
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          int pc = (cj[u] >= 0 && sub < sk_chunks) ? popc_u4(v[u], mine) : 0;
+          int pc = (sl[u] >= 0 && sub < sk_chunks) ? popc_u4(v[u], mine) : 0;
           pc += __shfl_xor_sync(0xffffffffu, pc, 1);
           pc += __shfl_xor_sync(0xffffffffu, pc, 2);
           pc += __shfl_xor_sync(0xffffffffu, pc, 4);
-          const int j = base + u * kGroups;
-          if (sub == 0 && j < KK) {
-            if (cj[u] >= 0) {
-              const int h = 1024 - pc;
-              cand_h[j] = uint16_t(h);
-              atomicAdd(&hist[h], 1u);
-              ++local_cnt;
-            } else {
-              cand_h[j] = 0xffff;
-            }
-          }
+          if (sub == 0 && sl[u] >= 0) meta[sl[u]] = (uint32_t(1024 - pc) << 16) | (meta[sl[u]] & kFirstMask);
         }
       }
-      if (local_cnt) atomicAdd(&s_cnt, local_cnt);
     }
     __syncthreads();
-    // ---- D
+    // ---- D  histogram over occurrences, threshold
+    for (int j = tid; j < KK; j += kThreads) {
+      const int sl = cand_slot[j];
+      if (sl >= 0) atomicAdd(&hist[(meta[sl] >> 16) & 0x7ffu], 1u);
+    }
+    __syncthreads();
     const int cnt = s_cnt;
-    my_cands += unsigned(cnt);
+    my_cands += unsigned(nu);
     if (cnt > R) {
       if (warp == 0) {
         const int per = (kHBins + 31) / 32;
@@ -212,7 +281,7 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
         }
       }
     } else if (tid == 0) {
-      s_ht = -1;  // everything valid is selected
+      s_ht = -1;  // every occurrence is selected
       s_gt = cnt;
     }
     __syncthreads();
@@ -223,7 +292,10 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
       const int j0 = tid * seg, j1 = min(KK, j0 + seg);
       int eq = 0;
       if (ht >= 0)
-        for (int j = j0; j < j1; ++j) eq += (cand_h[j] == ht) ? 1 : 0;
+        for (int j = j0; j < j1; ++j) {
+          const int sl = cand_slot[j];
+          eq += (sl >= 0 && int((meta[sl] >> 16) & 0x7ffu) == ht) ? 1 : 0;
+        }
       int incl = eq;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -235,12 +307,11 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
       int rank = incl - eq;
       for (int w = 0; w < warp; ++w) rank += s_wsum[w];
       for (int j = j0; j < j1; ++j) {
-        const int h = cand_h[j];
-        if (h == 0xffff) continue;
+        const int sl = cand_slot[j];
+        if (sl < 0) continue;
+        const int h = int((meta[sl] >> 16) & 0x7ffu);
         bool take;
-        if (ht < 0) {
-          take = true;
-        } else if (h > ht) {
+        if (ht < 0 || h > ht) {
           take = true;
         } else if (h == ht) {
           take = rank < need_eq;
@@ -248,34 +319,29 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
         } else {
           take = false;
         }
-        if (take) sel[atomicAdd(&s_nsel, 1)] = uint16_t(j);
+        if (take) atomicOr(&meta[sl], kSelFlag);
       }
     }
     __syncthreads();
-    // ---- F1  drop ids present in the starting pool with a real score
-    const int nsel = s_nsel;
-    for (int s = tid; s < nsel; s += kThreads) {
-      const int j = sel[s];
-      const int32_t id = cand_id[j];
-      bool skip = false;
-      for (int k = 0; k < K; ++k)
-        if (pool_id[k] == id && pool_sc[k] != kScoreMinI) skip = true;
-      if (!skip) need[atomicAdd(&s_nneed, 1)] = uint16_t(j);
+    // ---- F1  selected ids that are not starting-list members need a dot
+    for (int q = tid; q < nu; q += kThreads) {
+      const int sl = ulist[q];
+      if ((meta[sl] & kSelFlag) && !(uint32_t(key[sl]) & kPoolFlag)) need[atomicAdd(&s_nneed, 1)] = int16_t(sl);
     }
     __syncthreads();
-    // ---- F2  dots (8 lanes per candidate; a lane keeps up to eight 16-byte
-    //           loads of the candidate row in flight; own row from shared memory)
+    // ---- F2  dots (8 lanes per candidate, up to eight 16-byte loads in flight per lane)
     {
       const int nneed = s_nneed;
       my_dots += unsigned(nneed);
       const int32_t thr0 = pool_sc[K - 1];
       const int per_lane = d / 128;
       for (int wbase = warp * 4; wbase < nneed; wbase += kGroups) {
-        const int q = wbase + (lane >> 3);
-        const int j = q < nneed ? int(need[q]) : -1;
+        const int q = wbase + slot8;
+        const int sl = q < nneed ? int(need[q]) : -1;
+        const int32_t id = sl >= 0 ? int32_t(uint32_t(key[sl]) & 0x7fffffffu) : 0;
         int acc = 0;
-        if (j >= 0) {
-          const uint4* row = reinterpret_cast<const uint4*>(codes + int64_t(cand_id[j]) * d);
+        if (sl >= 0) {
+          const uint4* row = reinterpret_cast<const uint4*>(codes + int64_t(id) * d);
           uint4 v[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u)
@@ -287,16 +353,17 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
         acc += __shfl_xor_sync(0xffffffffu, acc, 1);
         acc += __shfl_xor_sync(0xffffffffu, acc, 2);
         acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-        if (sub == 0 && j >= 0 && acc > thr0) {
+        if (sub == 0 && sl >= 0 && acc > thr0) {
+          const uint32_t m = meta[sl];
           const int slot = atomicAdd(&s_nprom, 1);
-          pkey[slot] = (uint32_t(cand_h[j]) << 12) | uint32_t(4095 - j);
-          pid[slot] = cand_id[j];
+          pkey[slot] = (((m >> 16) & 0x7ffu) << 13) | (kFirstMask - (m & kFirstMask));
+          pid[slot] = id;
           pdot[slot] = acc;
         }
       }
     }
     __syncthreads();
-    // ---- G  rank sort (keys are distinct)
+    // ---- G  rank sort by (h desc, first j asc); keys are distinct
     const int P = s_nprom;
     for (int p = tid; p < P; p += kThreads) {
       const uint32_t kp = pkey[p];
