@@ -167,8 +167,9 @@ def recall_sample(x, knns, rows=10_000, seed=7):
     return synth.recall_at_k(kh, gt, rows=idx.cpu().numpy())
 
 
-def cpu_port_step(threads, sample=CPU_SAMPLE, seed=4242):
-    """One reference-algorithm build (oracle port, OpenMP) on the bounded sample; returns (s, n)."""
+def cpu_port_step(threads, sample=CPU_SAMPLE, seed=4242, want=False):
+    """One reference-algorithm build (oracle port, OpenMP, reference tie rules and
+    in-place race) on the bounded sample; returns (s, n[, x, knns])."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     import synth
@@ -177,8 +178,24 @@ def cpu_port_step(threads, sample=CPU_SAMPLE, seed=4242):
     x = synth.mixture(n, d, c, seed=seed)
     prm = oracle.params(threads=threads)
     t0 = time.perf_counter()
-    oracle.build_graph(x, prm)
-    return time.perf_counter() - t0, n
+    knns, _, _ = oracle.build_graph(x, prm)
+    el = time.perf_counter() - t0
+    return (el, n, x, knns) if want else (el, n)
+
+
+def recall_parity(x_np, ref_knns, dev):
+    """recall@15 (all rows, exact fp64) of the reference port's graph and of the
+    GPU build of the same rows: the benchmark spec's parity measure."""
+    import torch
+
+    import knng
+
+    x = torch.from_numpy(x_np).to(dev)
+    with knng.Context() as ctx:
+        kg, _, _ = ctx.build(x)
+    r_ref = recall_sample(x, torch.from_numpy(ref_knns), rows=x.shape[0])
+    r_gpu = recall_sample(x, kg, rows=x.shape[0])
+    return {"n": int(x.shape[0]), "reference_port": r_ref, "gpu": r_gpu, "gap_pt": 100 * (r_ref - r_gpu)}
 
 
 def run_reference(args):
@@ -285,9 +302,11 @@ def run_gpu(args):
     rec = recall_sample(x, knns, rows=args.recall_rows) if args.recall_rows > 0 and rank == 0 else None
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
+    parity = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
         threads = os.cpu_count() or 1
-        s, ns = cpu_port_step(threads)
+        s, ns, xs, ks = cpu_port_step(threads, want=True)
+        parity = recall_parity(xs, ks, dev)
         cpu = {"value": ns / s, "unit": "vectors/s", "cores": threads, "kind": "port",
                "sample": f"{CPU_SAMPLE[0]} x {CPU_SAMPLE[1]} rows ({CPU_SAMPLE[2]} centres), one whole build, "
                          "oracle restatement of src/main.cpp with OpenMP"}
@@ -304,7 +323,7 @@ def run_gpu(args):
             "build_s": last.build_s, "step_s": last.device_s, "iterations": it,
             "stage_s": {"quantize": last.quantize_s, "forest": last.forest_s, "init": last.init_s,
                         "join": last.join_s, "export": last.export_s},
-            "recall@15": rec, "recall_rows": args.recall_rows,
+            "recall@15": rec, "recall_rows": args.recall_rows, "recall_parity_100k": parity,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clk.summary(), "gpu_launches": launches, "wall_s": wall,
         }

@@ -35,13 +35,15 @@
 //      starting list's ids with a real score, flagged (bit 31 of the key)
 //   B  two-hop ids: warp per neighbour row (K contiguous ids), insert each,
 //      record its slot per j and the first j per slot (atomicMin)
-//   C  compact the distinct candidate slots; Hamming once per distinct id:
+//   C  Hamming once per distinct id (the first occurrence of an id appends
+//      its slot to the distinct list during B):
 //      8 lanes per candidate, one 16-byte sketch chunk per lane (128-byte
 //      rows = one line per candidate), warp __popc
 //   D  histogram of h over all occurrences, threshold h_t (warp scan)
 //   E  selection: every occurrence with h > h_t plus the first
-//      R - count(h > h_t) occurrences with h == h_t in j order (one block scan
-//      of per-thread tie counts); marks the selected slots
+//      R - count(h > h_t) occurrences with h == h_t in j order; one block scan
+//      of per-thread tie counts finds the cut position, then each distinct id
+//      is selected from its h and first j
 //   F  selected ids not flagged as starting-list members: dp4a dots, 8 lanes
 //      per candidate; keep those above the starting pool[K-1].score
 //   G  rank-sort the survivors by (h desc, first j asc)
@@ -62,7 +64,6 @@ constexpr int kHBins = 1025;
 constexpr int32_t kEmpty = 0x7fffffff;     // never a valid id (num_trees * n < 2^31)
 constexpr uint32_t kPoolFlag = 0x80000000u; // key bit: id is in the starting list with a real score
 constexpr uint32_t kFirstMask = 0x1fffu;    // meta bits 0..12: first j (8191 = none)
-constexpr uint32_t kSelFlag = 0x80000000u;  // meta bit 31: selected for rerank
 
 struct JoinSmem {
   int K, R, KK, d, W, HT;
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
   uint16_t* order = reinterpret_cast<uint16_t*>(smem + L.o_order);
   int32_t* pool_id = reinterpret_cast<int32_t*>(smem + L.o_pool_id);
   int32_t* pool_sc = reinterpret_cast<int32_t*>(smem + L.o_pool_sc);
-  __shared__ int s_cnt, s_ht, s_gt, s_nu, s_nneed, s_nprom;
+  __shared__ int s_cnt, s_ht, s_gt, s_jcut, s_nu, s_nneed, s_nprom;
   __shared__ int32_t s_wsum[kWarps];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, sub = lane & 7, slot8 = lane >> 3;
@@ -172,9 +173,9 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
     for (int c = tid; c < nchunk; c += kThreads) my_code[c] = reinterpret_cast<const uint4*>(codes + i * d)[c];
     for (int c = tid; c < sk_chunks; c += kThreads) my_sk[c] = reinterpret_cast<const uint4*>(sketch + i * W)[c];
     for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;
-    for (int t = tid; t < L.HT; t += kThreads) {
-      key[t] = kEmpty;
-      meta[t] = kFirstMask;
+    for (int t = tid; t < L.HT / 4; t += kThreads) {
+      reinterpret_cast<uint4*>(key)[t] = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
+      reinterpret_cast<uint4*>(meta)[t] = make_uint4(kFirstMask, kFirstMask, kFirstMask, kFirstMask);
     }
     if (tid == 0) {
       s_cnt = 0;
@@ -188,33 +189,43 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
       if (pool_sc[k] != kScoreMinI && id >= 0 && id < n) table_insert(key, mask, id, kPoolFlag);
     }
     __syncthreads();
-    // ---- B  (warp per neighbour row; no division)
-    int local_cnt = 0;
-    for (int k = warp; k < K; k += kWarps) {
-      const int32_t n1 = pool_id[k];
-      const bool ok = n1 >= 0 && n1 < n;
-      for (int k2 = lane; k2 < K; k2 += 32) {
-        const int j = k * K + k2;
-        int32_t n2 = ok ? ids_in[int64_t(n1) * K + k2] : -1;
-        int sl = -1;
-        if (n2 >= 0 && n2 < n && n2 != i) sl = table_insert(key, mask, n2, 0u);
-        cand_slot[j] = int16_t(sl);
-        if (sl >= 0) {
-          atomicMin(&meta[sl], uint32_t(j));
-          ++local_cnt;
-        }
+    // ---- B  (warp per neighbour row, all of the warp's rows loaded first; the
+    //         first occurrence to touch a slot appends it to the distinct list)
+    {
+      constexpr int kRowsPerWarp = kMaxK / kWarps;  // 8
+      int32_t v[2 * kRowsPerWarp];
+#pragma unroll
+      for (int t = 0; t < kRowsPerWarp; ++t) {
+        const int k = warp + kWarps * t;
+        const int32_t n1 = k < K ? pool_id[k] : -1;
+        const bool ok = n1 >= 0 && n1 < n;
+        v[2 * t] = (ok && lane < K) ? ids_in[int64_t(n1) * K + lane] : -1;
+        v[2 * t + 1] = (ok && lane + 32 < K) ? ids_in[int64_t(n1) * K + lane + 32] : -1;
       }
-    }
-    if (local_cnt) atomicAdd(&s_cnt, local_cnt);
-    __syncthreads();
-    // ---- C0  distinct candidate slots (touched by an occurrence)
-    for (int t = tid; t < L.HT; t += kThreads) {
-      const bool touched = (meta[t] & kFirstMask) != kFirstMask;
-      const unsigned bal = __ballot_sync(0xffffffffu, touched);
-      int base = 0;
-      if (lane == 0 && bal) base = atomicAdd(&s_nu, __popc(bal));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (touched) ulist[base + __popc(bal & ((1u << lane) - 1u))] = int16_t(t);
+      int local_cnt = 0;
+#pragma unroll
+      for (int t = 0; t < 2 * kRowsPerWarp; ++t) {
+        const int k = warp + kWarps * (t >> 1);
+        const int k2 = lane + 32 * (t & 1);
+        const int32_t n2 = v[t];
+        int sl = -1;
+        bool first = false;
+        if (k < K && k2 < K) {
+          const int j = k * K + k2;
+          if (n2 >= 0 && n2 < n && n2 != i) sl = table_insert(key, mask, n2, 0u);
+          cand_slot[j] = int16_t(sl);
+          if (sl >= 0) {
+            first = atomicMin(&meta[sl], uint32_t(j)) == kFirstMask;
+            ++local_cnt;
+          }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, first);
+        int base = 0;
+        if (lane == 0 && bal) base = atomicAdd(&s_nu, __popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (first) ulist[base + __popc(bal & ((1u << lane) - 1u))] = int16_t(sl);
+      }
+      if (local_cnt) atomicAdd(&s_cnt, local_cnt);
     }
     __syncthreads();
     // ---- C  Hamming once per distinct id (groups of 8 lanes, 4 in flight)
@@ -255,48 +266,12 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
     const int cnt = s_cnt;
     my_cands += unsigned(nu);
     if (cnt > R) {
-      if (warp == 0) {
-        const int per = (kHBins + 31) / 32;
-        const int lo = lane * per, hi = min(kHBins, lo + per);
-        int sum = 0;
-        for (int x = lo; x < hi; ++x) sum += int(hist[1024 - x]);
-        int incl = sum;
+      // bins from h = 1024 down: thread t sums bins 4t..4t+3 (index x = 1024 - h);
+      // bin x = 1024 (h = 0) is handled last
+      int sum = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int t = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += t;
-        }
-        const int excl = incl - sum;
-        if (excl < R && R <= incl) {
-          int run = excl;
-          for (int x = lo; x < hi; ++x) {
-            const int c = int(hist[1024 - x]);
-            if (run + c >= R) {
-              s_ht = 1024 - x;
-              s_gt = run;
-              break;
-            }
-            run += c;
-          }
-        }
-      }
-    } else if (tid == 0) {
-      s_ht = -1;  // every occurrence is selected
-      s_gt = cnt;
-    }
-    __syncthreads();
-    // ---- E  (thread-contiguous segments keep the j order for the tie ranks)
-    {
-      const int ht = s_ht, need_eq = R - s_gt;
-      const int seg = (KK + kThreads - 1) / kThreads;
-      const int j0 = tid * seg, j1 = min(KK, j0 + seg);
-      int eq = 0;
-      if (ht >= 0)
-        for (int j = j0; j < j1; ++j) {
-          const int sl = cand_slot[j];
-          eq += (sl >= 0 && int((meta[sl] >> 16) & 0x7ffu) == ht) ? 1 : 0;
-        }
-      int incl = eq;
+      for (int u = 0; u < 4; ++u) sum += int(hist[1024 - (4 * tid + u)]);
+      int incl = sum;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int t = __shfl_up_sync(0xffffffffu, incl, o);
@@ -304,29 +279,77 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
       }
       if (lane == 31) s_wsum[warp] = incl;
       __syncthreads();
-      int rank = incl - eq;
-      for (int w = 0; w < warp; ++w) rank += s_wsum[w];
-      for (int j = j0; j < j1; ++j) {
-        const int sl = cand_slot[j];
-        if (sl < 0) continue;
-        const int h = int((meta[sl] >> 16) & 0x7ffu);
-        bool take;
-        if (ht < 0 || h > ht) {
-          take = true;
-        } else if (h == ht) {
-          take = rank < need_eq;
-          ++rank;
-        } else {
-          take = false;
+      int before = 0;
+      for (int w = 0; w < warp; ++w) before += s_wsum[w];
+      const int excl = before + incl - sum;
+      if (excl < R && R <= excl + sum) {
+        int run = excl;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int c = int(hist[1024 - (4 * tid + u)]);
+          if (run + c >= R) {
+            s_ht = 1024 - (4 * tid + u);
+            s_gt = run;
+            break;
+          }
+          run += c;
         }
-        if (take) atomicOr(&meta[sl], kSelFlag);
+      }
+      if (tid == kThreads - 1 && excl + sum < R) {  // the cut falls in bin h = 0
+        s_ht = 0;
+        s_gt = excl + sum;
+      }
+    } else if (tid == 0) {
+      s_ht = -1;  // every occurrence is selected
+      s_gt = cnt;
+    }
+    __syncthreads();
+    // ---- E  tie cut: the j of the (R - count(h > h_t))-th occurrence with h == h_t
+    //         (thread-contiguous segments keep the j order); a distinct id with
+    //         h == h_t is selected iff its first occurrence is at or before it
+    {
+      const int ht = s_ht, need_eq = R - s_gt;
+      if (ht >= 0) {
+        const int seg = (KK + kThreads - 1) / kThreads;
+        const int j0 = tid * seg, j1 = min(KK, j0 + seg);
+        int eq = 0;
+        for (int j = j0; j < j1; ++j) {
+          const int sl = cand_slot[j];
+          eq += (sl >= 0 && int((meta[sl] >> 16) & 0x7ffu) == ht) ? 1 : 0;
+        }
+        int incl = eq;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        __syncthreads();  // s_wsum was read by the threshold step
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        int rank = incl - eq;
+        for (int w = 0; w < warp; ++w) rank += s_wsum[w];
+        if (rank < need_eq && need_eq <= rank + eq) {
+          for (int j = j0; j < j1; ++j) {
+            const int sl = cand_slot[j];
+            if (sl >= 0 && int((meta[sl] >> 16) & 0x7ffu) == ht && ++rank == need_eq) {
+              s_jcut = j;
+              break;
+            }
+          }
+        }
       }
     }
     __syncthreads();
-    // ---- F1  selected ids that are not starting-list members need a dot
-    for (int q = tid; q < nu; q += kThreads) {
-      const int sl = ulist[q];
-      if ((meta[sl] & kSelFlag) && !(uint32_t(key[sl]) & kPoolFlag)) need[atomicAdd(&s_nneed, 1)] = int16_t(sl);
+    // ---- F1  selected distinct ids that are not starting-list members need a dot
+    {
+      const int ht = s_ht, jcut = ht >= 0 ? s_jcut : 0;
+      for (int q = tid; q < nu; q += kThreads) {
+        const int sl = ulist[q];
+        const uint32_t m = meta[sl];
+        const int h = int((m >> 16) & 0x7ffu);
+        const bool sel = ht < 0 || h > ht || (h == ht && int(m & kFirstMask) <= jcut);
+        if (sel && !(uint32_t(key[sl]) & kPoolFlag)) need[atomicAdd(&s_nneed, 1)] = int16_t(sl);
+      }
     }
     __syncthreads();
     // ---- F2  dots (8 lanes per candidate, up to eight 16-byte loads in flight per lane)
