@@ -61,6 +61,8 @@ typedef struct knng_params {
   int row_order;         /* KNNG_ORDER_LEAF: process rows in tree-0 leaf order */
   uint32_t seed;         /* 1337: src/main.cpp:210 (trees), :271 (fills) */
   int device;            /* CUDA device ordinal */
+  int autotune;          /* 1: time the join configurations once per (d, size) */
+  int use_graph;         /* 1: replay the NN-Descent phase as a CUDA graph */
 } knng_params;
 
 /* Per-build timings and convergence record (seconds, device-timed). */
@@ -81,7 +83,24 @@ typedef struct knng_stats {
   int64_t join_candidates[64]; /* sketch candidates scored per iteration */
   int64_t join_dots[64];  /* int8 rows reranked per iteration */
   int64_t kernel_launches;/* libknng kernels launched by the call */
+  int join_ctas_per_sm;   /* autotuned join configuration used */
+  int join_cblock;
+  int graph_used;         /* NN-Descent phase ran as a CUDA graph */
 } knng_stats;
+
+/* One job of a batch (knng_build_batch).  Inputs as for knng_build; status
+ * and iterations are written back. */
+typedef struct knng_job {
+  const void* rows;
+  int64_t n;
+  int d;
+  int rows_on_device;
+  int32_t* knns;
+  float* dists;
+  int out_on_device;
+  int status;      /* out: KNNG_OK or the error of the job's group */
+  int iterations;  /* out: NN-Descent iterations the job ran */
+} knng_job;
 
 typedef struct knng_ctx knng_ctx;
 
@@ -107,6 +126,16 @@ void knng_destroy(knng_ctx* ctx);
  * fully written before the call (it does not wait for other streams). */
 int knng_build(knng_ctx* ctx, const void* rows, int64_t n, int d, int rows_on_device,
                int32_t* knns, float* dists, int out_on_device, knng_stats* stats);
+
+/* Batched builds (no counterpart in the reference, which builds one graph per
+ * process): independent jobs of any n and d are built together, jobs of equal
+ * d as one problem laid out back to back -- one forest pass, one leaf Gram and
+ * merge, one persistent join launch per iteration over every job's rows, the
+ * NN-Descent phase replayed as a CUDA graph.  Each job keeps its own pivots,
+ * random fills and early stop (src/main.cpp:432-439), so its knns/dists are
+ * bit-identical to knng_build of that job alone.  stats (may be NULL) sums
+ * the groups. */
+int knng_build_batch(knng_ctx* ctx, knng_job* jobs, int count, knng_stats* stats);
 
 /* Text for a status code, and the last detailed error message of ctx. */
 const char* knng_status_string(int status);

@@ -18,6 +18,8 @@
 #include <vector>
 
 #include <atomic>
+#include <cmath>
+#include <map>
 
 namespace knng {
 size_t join_smem_bytes(int K, int R, int d);
@@ -29,6 +31,8 @@ void note_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 }  // namespace knng
 
 using namespace knng;
+
+constexpr int kMaxIterEvents = 2 * 64 + 2;
 
 struct DevBuf {
   void* p = nullptr;
@@ -60,8 +64,14 @@ struct knng_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   cudaEvent_t jev[2] = {};
+  cudaEvent_t itev[kMaxIterEvents] = {};
   std::string last_error;
-  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars;
+  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs;
+  // join phase captured as a CUDA graph, reused while the launch key matches
+  cudaGraphExec_t join_graph = nullptr;
+  std::vector<uintptr_t> join_graph_key;
+  // autotuned join configuration per (d, log2 rows): (ctas_per_sm, cblock)
+  std::map<std::pair<int, int>, std::pair<int, int>> tuned;
 };
 
 namespace {
@@ -158,18 +168,33 @@ int ensure_scratch(knng_ctx* c, int64_t n, Scratch* s, int64_t n_replay) {
   return KNNG_OK;
 }
 
+// Job table of one job covering all n rows (stage entry points).
+int single_job(knng_ctx* c, int64_t n, JobTable* jt) {
+  cudaError_t e = c->jobs.ensure(64);
+  if (e) return cuda_fail(c, e, "job table allocation");
+  const int32_t h[2] = {0, int32_t(n)};
+  if ((e = cudaMemcpyAsync(c->jobs.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream)) ||
+      (e = cudaStreamSynchronize(c->stream)))
+    return cuda_fail(c, e, "job table upload");
+  jt->count = 1;
+  jt->off = c->jobs.as<int32_t>(0);
+  jt->n = c->jobs.as<int32_t>(4);
+  return KNNG_OK;
+}
+
 float elapsed(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0.f;
   cudaEventElapsedTime(&ms, a, b);
   return ms;
 }
 
-int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_device) {
+int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_device, int64_t row0 = 0) {
   const int W = d / 64;
   cudaError_t e;
+  int8_t* codes = c->codes.as<int8_t>() + row0 * d;
+  uint64_t* sketch = c->sketch.as<uint64_t>() + row0 * W;
   if (on_device) {
-    e = launch_quantize(static_cast<const float*>(rows), n, d, c->prm.quant_mode, c->codes.as<int8_t>(),
-                        c->sketch.as<uint64_t>(), c->stream);
+    e = launch_quantize(static_cast<const float*>(rows), n, d, c->prm.quant_mode, codes, sketch, c->stream);
     return e ? cuda_fail(c, e, "quantize") : KNNG_OK;
   }
   // Host rows: stream fixed-size chunks through two staging buffers so the
@@ -183,10 +208,257 @@ int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_devic
     float* stage = c->staging.as<float>((k & 1) * chunk_bytes);
     if ((e = cudaMemcpyAsync(stage, src + off * d, size_t(m) * d * 4, cudaMemcpyHostToDevice, c->stream)))
       return cuda_fail(c, e, "input copy");
-    if ((e = launch_quantize(stage, m, d, c->prm.quant_mode, c->codes.as<int8_t>() + off * d,
-                             c->sketch.as<uint64_t>() + off * W, c->stream)))
+    if ((e = launch_quantize(stage, m, d, c->prm.quant_mode, codes + off * d, sketch + off * W, c->stream)))
       return cuda_fail(c, e, "quantize");
   }
+  return KNNG_OK;
+}
+
+struct BJob {
+  const void* rows;
+  int64_t n;
+  int on_dev;
+  int32_t* knns;
+  float* dists;
+  int out_dev;
+  int iterations;  // out
+};
+
+// Times the join configurations on the batch's initial graph (output to the
+// spare buffer, which iteration 0 overwrites) and keeps the fastest per
+// (d, log2 rows).  Returns (ctas_per_sm, cblock).
+std::pair<int, int> autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int32_t* const scs[2],
+                                  const int32_t* order, unsigned long long* scratch_counters) {
+  const knng_params& p = c->prm;
+  const auto key = std::make_pair(d, int(std::log2(double(N))));
+  auto it = c->tuned.find(key);
+  if (it != c->tuned.end()) return it->second;
+  std::pair<int, int> best{4, 4};
+  if (!p.autotune || p.join_mode != KNNG_JOIN_JACOBI) return best;
+  const std::pair<int, int> cand[] = {{4, 4}, {4, 8}, {3, 4}, {3, 8}, {4, 2}};
+  float best_ms = 1e30f;
+  const int K = p.k_build;
+  for (const auto& cf : cand) {
+    cudaEventRecord(c->jev[0], c->stream);
+    if (launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
+                    ids[1], scs[1], order, scratch_counters, c->num_sms, c->stream, nullptr, nullptr, cf.first,
+                    cf.second) != cudaSuccess)
+      break;
+    cudaEventRecord(c->jev[1], c->stream);
+    cudaEventSynchronize(c->jev[1]);
+    const float ms = elapsed(c->jev[0], c->jev[1]);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = cf;
+    }
+  }
+  c->tuned[key] = best;
+  return best;
+}
+
+// The NN-Descent phase: max_iterations launches of the join, each followed by
+// the per-job stop check; launches after every job has stopped do nothing.
+cudaError_t join_phase(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int32_t* const scs[2],
+                       const int32_t* order, const JobTable& jt, const JoinCtl& ctl, unsigned long long* counters,
+                       std::pair<int, int> cfg, bool capture) {
+  const knng_params& p = c->prm;
+  const int K = p.k_build;
+  const bool jac = p.join_mode == KNNG_JOIN_JACOBI;
+  cudaError_t e;
+  int cur = 0;
+  for (int it = 0; it < p.max_iterations; ++it) {
+    const int nxt = jac ? 1 - cur : cur;
+    e = capture ? cudaEventRecordWithFlags(c->itev[2 * it], c->stream, cudaEventRecordExternal)
+                : cudaEventRecord(c->itev[2 * it], c->stream);
+    if (e) return e;
+    if ((e = launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[cur],
+                         scs[cur], ids[nxt], scs[nxt], order, counters + 3 * it, c->num_sms, c->stream, &jt, &ctl,
+                         cfg.first, cfg.second)))
+      return e;
+    e = capture ? cudaEventRecordWithFlags(c->itev[2 * it + 1], c->stream, cudaEventRecordExternal)
+                : cudaEventRecord(c->itev[2 * it + 1], c->stream);
+    if (e) return e;
+    if ((e = launch_stop_check(jt, ctl, K, it, nxt, p.early_stop_rate, p.rate_diff_tol, c->stream))) return e;
+    cur = nxt;
+  }
+  return cudaSuccess;
+}
+
+// One problem made of J jobs of the same dimension d (a single build is J = 1).
+int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
+  using clk = std::chrono::steady_clock;
+  const auto t_start = clk::now();
+  const int64_t launches0 = launches();
+  const knng_params& p = c->prm;
+  const int K = p.k_build, T = p.num_trees, W = d / 64, MI = p.max_iterations;
+  std::memset(&S, 0, sizeof(S));
+  std::vector<int32_t> hoff(J), hn(J);
+  int64_t N = 0;
+  int split = 0;
+  for (int b = 0; b < J; ++b) {
+    hoff[b] = int32_t(N);
+    hn[b] = int32_t(jobs[b].n);
+    N += jobs[b].n;
+    if (jobs[b].n > p.leaf_size) ++split;
+  }
+  if (int64_t(T) * N > INT32_MAX) return set_error(c, KNNG_E_ARGS, "num_trees * total rows must fit in int32");
+  cudaError_t e;
+  const size_t nk = size_t(N) * K;
+  if ((e = c->codes.ensure(size_t(N) * d)) || (e = c->sketch.ensure(size_t(N) * W * 8)) ||
+      (e = c->graph.ensure(nk * 16)) || (e = c->perm.ensure(size_t(T) * N * 4)) ||
+      (e = c->leaf_flag.ensure(size_t(T) * N)))
+    return cuda_fail(c, e, "device allocation");
+  Scratch s;
+  int st = ensure_scratch(c, N, &s, 0);
+  if (st) return st;
+  // job table + NN-Descent control block
+  const size_t jb = size_t(J);
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = o;
+    o += (bytes + 15) & ~size_t(15);
+    return at;
+  };
+  const size_t o_off = take(jb * 4), o_n = take(jb * 4), o_upd = take(jb * 8), o_done = take(jb * 4),
+               o_prev = take(jb * 4), o_iters = take(jb * 4), o_flags = take(16), o_log = take(size_t(MI + 1) * jb * 8),
+               o_cnt = take(size_t(MI + 1) * 3 * 8);
+  if ((e = c->jobs.ensure(o))) return cuda_fail(c, e, "job table allocation");
+  cudaStream_t str = c->stream;
+  if ((e = cudaMemsetAsync(c->jobs.p, 0, o, str)) ||
+      (e = cudaMemcpyAsync(c->jobs.as<int32_t>(o_off), hoff.data(), jb * 4, cudaMemcpyHostToDevice, str)) ||
+      (e = cudaMemcpyAsync(c->jobs.as<int32_t>(o_n), hn.data(), jb * 4, cudaMemcpyHostToDevice, str)))
+    return cuda_fail(c, e, "job table upload");
+  JobTable jt;
+  jt.count = J;
+  jt.off = c->jobs.as<int32_t>(o_off);
+  jt.n = c->jobs.as<int32_t>(o_n);
+  JoinCtl ctl;
+  ctl.counters = c->jobs.as<unsigned long long>(o_cnt);
+  ctl.job_upd = c->jobs.as<unsigned long long>(o_upd);
+  ctl.job_done = c->jobs.as<int>(o_done);
+  ctl.job_prev = c->jobs.as<float>(o_prev);
+  ctl.job_iters = c->jobs.as<int>(o_iters);
+  ctl.all_done = c->jobs.as<int>(o_flags);
+  ctl.final_buf = c->jobs.as<int>(o_flags) + 1;
+  ctl.upd_log = c->jobs.as<long long>(o_log);
+  unsigned long long* tune_counters = ctl.counters + 3 * MI;
+  int32_t* ids[2] = {c->graph.as<int32_t>(0), c->graph.as<int32_t>(nk * 8)};
+  int32_t* scs[2] = {c->graph.as<int32_t>(nk * 4), c->graph.as<int32_t>(nk * 12)};
+
+  cudaEventRecord(c->ev[0], str);
+  for (int b = 0; b < J; ++b)
+    if ((st = quantize_input(c, jobs[b].rows, jobs[b].n, d, jobs[b].on_dev, hoff[b]))) return st;
+  cudaEventRecord(c->ev[1], str);
+  int64_t levels = 0, leaves = 0;
+  if ((st = run_forest(c->codes.as<int8_t>(), N, d, T, p.leaf_size, p.seed, nullptr, 0, c->perm.as<int32_t>(),
+                       c->leaf_flag.as<uint8_t>(), s.fb, str, &levels, &c->last_error, jt, split)))
+    return st;
+  cudaEventRecord(c->ev[2], str);
+  if ((st = run_init(c->codes.as<int8_t>(), N, d, T, p.leaf_size, K, p.seed, c->perm.as<int32_t>(),
+                     c->leaf_flag.as<uint8_t>(), ids[0], scs[0], s.ib, str, &leaves, &c->last_error, jt)))
+    return st;
+  const int32_t* order = p.row_order == KNNG_ORDER_LEAF ? c->perm.as<int32_t>() : nullptr;
+  const std::pair<int, int> cfg = autotune_join(c, N, d, ids, scs, order, tune_counters);
+  cudaEventRecord(c->ev[3], str);
+  // NN-Descent, captured once per launch key and replayed
+  bool graph_used = false;
+  if (p.use_graph) {
+    const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->sketch.p), uintptr_t(c->graph.p),
+                                        uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(N), uintptr_t(d),
+                                        uintptr_t(J), uintptr_t(o), uintptr_t(cfg.first), uintptr_t(cfg.second),
+                                        uintptr_t(p.row_order), uintptr_t(p.join_mode), uintptr_t(MI),
+                                        uintptr_t(K), uintptr_t(p.rerank_mult)};
+    if (!c->join_graph || c->join_graph_key != key) {
+      if (c->join_graph) {
+        cudaGraphExecDestroy(c->join_graph);
+        c->join_graph = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const cudaError_t ce = join_phase(c, N, d, ids, scs, order, jt, ctl, ctl.counters, cfg, true);
+        const cudaError_t ee = cudaStreamEndCapture(str, &g);
+        if (ce == cudaSuccess && ee == cudaSuccess && g &&
+            cudaGraphInstantiate(&c->join_graph, g, 0) == cudaSuccess)
+          c->join_graph_key = key;
+        else
+          c->join_graph = nullptr;
+        if (g) cudaGraphDestroy(g);
+      }
+      cudaGetLastError();
+    }
+    if (c->join_graph) {
+      if ((e = cudaGraphLaunch(c->join_graph, str))) return cuda_fail(c, e, "join graph launch");
+      graph_used = true;
+    }
+  }
+  if (!graph_used && (e = join_phase(c, N, d, ids, scs, order, jt, ctl, ctl.counters, cfg, false)))
+    return cuda_fail(c, e, "join phase");
+  cudaEventRecord(c->ev[4], str);
+  // results of the control block
+  std::vector<int> iters(jb);
+  std::vector<long long> log(size_t(MI) * jb);
+  std::vector<unsigned long long> cnt(size_t(MI) * 3);
+  int flags[2] = {0, 0};
+  if ((e = cudaMemcpyAsync(iters.data(), ctl.job_iters, jb * 4, cudaMemcpyDeviceToHost, str)) ||
+      (MI && (e = cudaMemcpyAsync(log.data(), ctl.upd_log, log.size() * 8, cudaMemcpyDeviceToHost, str))) ||
+      (MI && (e = cudaMemcpyAsync(cnt.data(), ctl.counters, cnt.size() * 8, cudaMemcpyDeviceToHost, str))) ||
+      (e = cudaMemcpyAsync(flags, ctl.all_done, 8, cudaMemcpyDeviceToHost, str)) ||
+      (e = cudaStreamSynchronize(str)))
+    return cuda_fail(c, e, "join phase");
+  const int fin = MI == 0 ? 0 : flags[1];
+  // export (job-local 1-based ids) and hand out each job's rows
+  const size_t outn = size_t(N) * p.k_eval;
+  int32_t* kd;
+  float* dd;
+  const bool direct = J == 1 && jobs[0].out_dev;
+  if (direct) {
+    kd = jobs[0].knns;
+    dd = jobs[0].dists;
+  } else {
+    if ((e = c->outbuf.ensure(outn * 8))) return cuda_fail(c, e, "output allocation");
+    kd = c->outbuf.as<int32_t>(0);
+    dd = c->outbuf.as<float>(outn * 4);
+  }
+  if ((e = launch_export(ids[fin], scs[fin], N, K, p.k_eval, nullptr, kd, dd, str, &jt)))
+    return cuda_fail(c, e, "export");
+  if (!direct)
+    for (int b = 0; b < J; ++b) {
+      const size_t cnt_b = size_t(jobs[b].n) * p.k_eval, at = size_t(hoff[b]) * p.k_eval;
+      const cudaMemcpyKind kind = jobs[b].out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+      if ((e = cudaMemcpyAsync(jobs[b].knns, kd + at, cnt_b * 4, kind, str)) ||
+          (e = cudaMemcpyAsync(jobs[b].dists, dd + at, cnt_b * 4, kind, str)))
+        return cuda_fail(c, e, "output copy");
+    }
+  cudaEventRecord(c->ev[5], str);
+  if ((e = cudaStreamSynchronize(str))) return cuda_fail(c, e, "build");
+  int max_it = 0;
+  for (int b = 0; b < J; ++b) {
+    jobs[b].iterations = iters[b];
+    max_it = std::max(max_it, iters[b]);
+  }
+  S.quantize_s = elapsed(c->ev[0], c->ev[1]) * 1e-3;
+  S.forest_s = elapsed(c->ev[1], c->ev[2]) * 1e-3;
+  S.init_s = elapsed(c->ev[2], c->ev[3]) * 1e-3;
+  S.join_s = elapsed(c->ev[3], c->ev[4]) * 1e-3;
+  S.export_s = elapsed(c->ev[4], c->ev[5]) * 1e-3;
+  S.build_s = elapsed(c->ev[1], c->ev[4]) * 1e-3;
+  S.device_s = elapsed(c->ev[0], c->ev[5]) * 1e-3;
+  S.iterations = max_it;
+  for (int it = 0; it < max_it && it < 64; ++it) {
+    long long u = 0;
+    for (int b = 0; b < J; ++b) u += log[size_t(it) * J + b];
+    S.updates[it] = u;
+    S.join_ms[it] = elapsed(c->itev[2 * it], c->itev[2 * it + 1]);
+    S.join_candidates[it] = int64_t(cnt[3 * it + 1]);
+    S.join_dots[it] = int64_t(cnt[3 * it + 2]);
+  }
+  S.forest_levels = levels;
+  S.leaves = leaves;
+  S.join_ctas_per_sm = cfg.first;
+  S.join_cblock = cfg.second;
+  S.graph_used = graph_used ? 1 : 0;
+  S.kernel_launches = launches() - launches0;
+  S.total_s = std::chrono::duration<double>(clk::now() - t_start).count();
   return KNNG_OK;
 }
 
@@ -209,6 +481,8 @@ void knng_default_params(knng_params* p) {
   p->row_order = KNNG_ORDER_LEAF;
   p->seed = 1337;
   p->device = 0;
+  p->autotune = 1;
+  p->use_graph = 1;
 }
 
 const char* knng_status_string(int s) {
@@ -259,6 +533,11 @@ int knng_create(knng_ctx** out, const knng_params* p) {
       knng_destroy(c);
       return KNNG_E_CUDA;
     }
+  for (auto& ev : c->itev)
+    if ((e = cudaEventCreate(&ev))) {
+      knng_destroy(c);
+      return KNNG_E_CUDA;
+    }
   *out = c;
   return KNNG_OK;
 }
@@ -267,9 +546,12 @@ void knng_destroy(knng_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->join_graph) cudaGraphExecDestroy(c->join_graph);
   for (DevBuf* b : {&c->codes, &c->sketch, &c->graph, &c->perm, &c->leaf_flag, &c->scratch, &c->staging,
-                    &c->outbuf, &c->scalars})
+                    &c->outbuf, &c->scalars, &c->jobs})
     b->release();
+  for (auto& ev : c->itev)
+    if (ev) cudaEventDestroy(ev);
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : c->jev)
@@ -296,8 +578,11 @@ int knng_forest(knng_ctx* c, const int8_t* codes_dev, int64_t n, int d, const in
   Scratch s;
   if ((st = ensure_scratch(c, n, &s, replay ? n_replay : 0))) return st;
   int64_t levels = 0;
+  JobTable jt;
+  if ((st = single_job(c, n, &jt))) return st;
   st = run_forest(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.seed, replay, replay ? n_replay : 0,
-                  perm_dev, leaf_flag_dev, s.fb, c->stream, &levels, &c->last_error);
+                  perm_dev, leaf_flag_dev, s.fb, c->stream, &levels, &c->last_error, jt,
+                  n > c->prm.leaf_size ? 1 : 0);
   if (st) return st;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   return e ? cuda_fail(c, e, "forest") : KNNG_OK;
@@ -311,8 +596,10 @@ int knng_init_graph(knng_ctx* c, const int8_t* codes_dev, int64_t n, int d, cons
   cudaSetDevice(c->device);
   Scratch s;
   if ((st = ensure_scratch(c, n, &s, 0))) return st;
+  JobTable jt;
+  if ((st = single_job(c, n, &jt))) return st;
   st = run_init(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.k_build, c->prm.seed, perm_dev,
-                leaf_flag_dev, ids_dev, scores_dev, s.ib, c->stream, nullptr, &c->last_error);
+                leaf_flag_dev, ids_dev, scores_dev, s.ib, c->stream, nullptr, &c->last_error, jt);
   if (st) return st;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   return e ? cuda_fail(c, e, "init") : KNNG_OK;
@@ -352,98 +639,67 @@ int knng_export(const int32_t* ids_dev, const int32_t* scores_dev, int64_t n, in
 
 int knng_build(knng_ctx* c, const void* rows, int64_t n, int d, int rows_on_device, int32_t* knns, float* dists,
                int out_on_device, knng_stats* stats) {
-  using clk = std::chrono::steady_clock;
-  const auto t_start = clk::now();
-  const int64_t launches0 = launches();
   if (!c || !rows || !knns || !dists) return set_error(c, KNNG_E_ARGS, "null argument");
   int st = check_shape(c, n, d);
   if (st) return st;
   cudaSetDevice(c->device);
-  const knng_params& p = c->prm;
-  const int K = p.k_build, T = p.num_trees, W = d / 64;
+  BJob j{rows, n, rows_on_device, knns, dists, out_on_device, 0};
+  knng_stats local{};
+  return run_batch(c, &j, 1, d, stats ? *stats : local);
+}
+
+int knng_build_batch(knng_ctx* c, knng_job* jobs, int count, knng_stats* stats) {
+  if (!c || !jobs || count < 1) return set_error(c, KNNG_E_ARGS, "null argument or empty batch");
+  for (int b = 0; b < count; ++b) {
+    if (!jobs[b].rows || !jobs[b].knns || !jobs[b].dists) return set_error(c, KNNG_E_ARGS, "null job buffer");
+    int st = check_shape(c, jobs[b].n, jobs[b].d);
+    if (st) return st;
+  }
+  cudaSetDevice(c->device);
   knng_stats local{};
   knng_stats& S = stats ? *stats : local;
   std::memset(&S, 0, sizeof(S));
-  cudaError_t e;
-  const size_t nk = size_t(n) * K;
-  if ((e = c->codes.ensure(size_t(n) * d)) || (e = c->sketch.ensure(size_t(n) * W * 8)) ||
-      (e = c->graph.ensure(nk * 16)) || (e = c->perm.ensure(size_t(T) * n * 4)) ||
-      (e = c->leaf_flag.ensure(size_t(T) * n)))
-    return cuda_fail(c, e, "device allocation");
-  Scratch s;
-  if ((st = ensure_scratch(c, n, &s, 0))) return st;
-  cudaStream_t str = c->stream;
-  int32_t* ids[2] = {c->graph.as<int32_t>(0), c->graph.as<int32_t>(nk * 8)};
-  int32_t* scs[2] = {c->graph.as<int32_t>(nk * 4), c->graph.as<int32_t>(nk * 12)};
-  cudaEventRecord(c->ev[0], str);
-  if ((st = quantize_input(c, rows, n, d, rows_on_device))) return st;
-  cudaEventRecord(c->ev[1], str);
-  int64_t levels = 0, leaves = 0;
-  if ((st = run_forest(c->codes.as<int8_t>(), n, d, T, p.leaf_size, p.seed, nullptr, 0, c->perm.as<int32_t>(),
-                       c->leaf_flag.as<uint8_t>(), s.fb, str, &levels, &c->last_error)))
-    return st;
-  cudaEventRecord(c->ev[2], str);
-  if ((st = run_init(c->codes.as<int8_t>(), n, d, T, p.leaf_size, K, p.seed, c->perm.as<int32_t>(),
-                     c->leaf_flag.as<uint8_t>(), ids[0], scs[0], s.ib, str, &leaves, &c->last_error)))
-    return st;
-  cudaEventRecord(c->ev[3], str);
-  unsigned long long* up = c->scalars.as<unsigned long long>(256);
-  const int32_t* order = p.row_order == KNNG_ORDER_LEAF ? c->perm.as<int32_t>() : nullptr;
-  int cur = 0, it = 0;
-  float prev = 1.0f;
-  for (; it < p.max_iterations; ++it) {
-    const int nxt = p.join_mode == KNNG_JOIN_JACOBI ? 1 - cur : cur;
-    unsigned long long h[3] = {0, 0, 0};
-    if ((e = cudaMemsetAsync(up, 0, 24, str)) || (e = cudaEventRecord(c->jev[0], str)) ||
-        (e = launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), n, d, K, K * p.rerank_mult, ids[cur],
-                         scs[cur], ids[nxt], scs[nxt], order, up, c->num_sms, str)) ||
-        (e = cudaEventRecord(c->jev[1], str)) ||
-        (e = cudaMemcpyAsync(h, up, 24, cudaMemcpyDeviceToHost, str)) || (e = cudaStreamSynchronize(str)))
-      return cuda_fail(c, e, "join iteration");
-    cur = nxt;
-    if (it < 64) {
-      S.updates[it] = int64_t(h[0]);
-      S.join_candidates[it] = int64_t(h[1]);
-      S.join_dots[it] = int64_t(h[2]);
-      S.join_ms[it] = elapsed(c->jev[0], c->jev[1]);
+  // one problem per dimension: jobs of equal d are laid out back to back
+  std::vector<int> dims;
+  for (int b = 0; b < count; ++b)
+    if (std::find(dims.begin(), dims.end(), jobs[b].d) == dims.end()) dims.push_back(jobs[b].d);
+  for (int d : dims) {
+    std::vector<BJob> group;
+    std::vector<int> idx;
+    for (int b = 0; b < count; ++b)
+      if (jobs[b].d == d) {
+        group.push_back(BJob{jobs[b].rows, jobs[b].n, jobs[b].rows_on_device, jobs[b].knns, jobs[b].dists,
+                             jobs[b].out_on_device, 0});
+        idx.push_back(b);
+      }
+    knng_stats gs{};
+    int st = run_batch(c, group.data(), int(group.size()), d, gs);
+    for (size_t g = 0; g < group.size(); ++g) {
+      jobs[idx[g]].status = st;
+      jobs[idx[g]].iterations = group[g].iterations;
     }
-    const float rate = float(h[0]) / float(uint64_t(n) * uint64_t(K));
-    if (rate < p.early_stop_rate || (it > 0 && (prev - rate) < p.rate_diff_tol)) {
-      ++it;
-      break;
+    if (st) return st;
+    S.quantize_s += gs.quantize_s;
+    S.forest_s += gs.forest_s;
+    S.init_s += gs.init_s;
+    S.join_s += gs.join_s;
+    S.export_s += gs.export_s;
+    S.build_s += gs.build_s;
+    S.device_s += gs.device_s;
+    S.kernel_launches += gs.kernel_launches;
+    S.forest_levels = std::max(S.forest_levels, gs.forest_levels);
+    S.leaves += gs.leaves;
+    S.iterations = std::max(S.iterations, gs.iterations);
+    for (int it = 0; it < 64; ++it) {
+      S.updates[it] += gs.updates[it];
+      S.join_ms[it] += gs.join_ms[it];
+      S.join_candidates[it] += gs.join_candidates[it];
+      S.join_dots[it] += gs.join_dots[it];
     }
-    prev = rate;
+    S.join_ctas_per_sm = gs.join_ctas_per_sm;
+    S.join_cblock = gs.join_cblock;
+    S.graph_used = gs.graph_used;
   }
-
-  cudaEventRecord(c->ev[4], str);
-  int32_t* kd = knns;
-  float* dd = dists;
-  const size_t outn = size_t(n) * p.k_eval;
-  if (!out_on_device) {
-    if ((e = c->outbuf.ensure(outn * 8))) return cuda_fail(c, e, "output allocation");
-    kd = c->outbuf.as<int32_t>(0);
-    dd = c->outbuf.as<float>(outn * 4);
-  }
-  if ((e = launch_export(ids[cur], scs[cur], n, K, p.k_eval, nullptr, kd, dd, str))) return cuda_fail(c, e, "export");
-  if (!out_on_device) {
-    if ((e = cudaMemcpyAsync(knns, kd, outn * 4, cudaMemcpyDeviceToHost, str)) ||
-        (e = cudaMemcpyAsync(dists, dd, outn * 4, cudaMemcpyDeviceToHost, str)))
-      return cuda_fail(c, e, "output copy");
-  }
-  cudaEventRecord(c->ev[5], str);
-  if ((e = cudaStreamSynchronize(str))) return cuda_fail(c, e, "build");
-  S.quantize_s = elapsed(c->ev[0], c->ev[1]) * 1e-3;
-  S.forest_s = elapsed(c->ev[1], c->ev[2]) * 1e-3;
-  S.init_s = elapsed(c->ev[2], c->ev[3]) * 1e-3;
-  S.join_s = elapsed(c->ev[3], c->ev[4]) * 1e-3;
-  S.export_s = elapsed(c->ev[4], c->ev[5]) * 1e-3;
-  S.build_s = elapsed(c->ev[1], c->ev[4]) * 1e-3;
-  S.iterations = it;
-  S.forest_levels = levels;
-  S.leaves = leaves;
-  S.device_s = elapsed(c->ev[0], c->ev[5]) * 1e-3;
-  S.kernel_launches = launches() - launches0;
-  S.total_s = std::chrono::duration<double>(clk::now() - t_start).count();
   return KNNG_OK;
 }
 

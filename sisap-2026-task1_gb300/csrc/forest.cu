@@ -16,6 +16,9 @@
 // (the right subtree's draws wait for the left subtree's), so it is replayed
 // only in tests, from the oracle's log.
 //
+// A batch of jobs is one problem of N rows (tree-major [T][N] arrays, job b at
+// offset off[b] in every tree); every level serves all jobs' nodes at once.
+//
 // Per level: pick_pivots -> scan(tiles) -> side (8 lanes per row, dp4a,
 // HBM-bound: d bytes read per active member) -> scan(left counts) -> scatter
 // (stable partition into perm_tmp) -> copy back -> children (leaf flags,
@@ -50,24 +53,34 @@ __global__ void init_perm(int32_t* perm, int64_t n, int T) {
     perm[i] = int32_t(i % n);
 }
 
-__global__ void root_nodes(NodeArr nd, int64_t n, int T, int leaf, uint8_t* leaf_flag) {
+// Roots: for tree t and job b the range t*N + off[b] of size n[b]; jobs with
+// n[b] <= leaf are single leaves.  Node order is by start (tree, then job).
+__global__ void root_nodes(NodeArr nd, int64_t N, int T, int leaf, uint8_t* leaf_flag, JobTable jt, int split_jobs) {
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    if (n > leaf) {
-      nd.start[t] = int32_t(int64_t(t) * n);
-      nd.size[t] = int32_t(n);
-    } else {
-      leaf_flag[int64_t(t) * n] = 1;
+    int k = t * split_jobs;
+    for (int b = 0; b < jt.count; ++b) {
+      const int64_t start = int64_t(t) * N + jt.off[b];
+      if (jt.n[b] > leaf) {
+        nd.start[k] = int32_t(start);
+        nd.size[k] = jt.n[b];
+        ++k;
+      } else {
+        leaf_flag[start] = 1;
+      }
     }
   }
 }
 
+// Node identity is job-local -- (tree, start within the job's range, size) --
+// so a job draws the same pivots alone and inside any batch.
 __global__ void pick_pivots(NodeArr nd, int cnt, int64_t n, uint32_t seed, int level, const int32_t* perm,
-                            const int32_t* replay, int32_t* tile_cnt, unsigned* err) {
+                            const int32_t* replay, int32_t* tile_cnt, unsigned* err, JobTable jt) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= cnt) return;
   const int32_t start = nd.start[k], size = nd.size[k];
   const int32_t tree = int32_t(int64_t(start) / n);
-  const int32_t local = int32_t(int64_t(start) - int64_t(tree) * n);
+  const int32_t in_tree = int32_t(int64_t(start) - int64_t(tree) * n);
+  const int32_t local = in_tree - jt.off[job_of(jt, in_tree)];
   int32_t p1, p2;
   if (replay) {
     const int32_t* r = replay + 6 * int64_t(k);
@@ -305,7 +318,7 @@ size_t forest_bytes(int64_t n, int T, int leaf, int64_t* max_nodes, int64_t* max
 
 int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t seed, const int32_t* replay_host,
                int64_t n_replay, int32_t* perm, uint8_t* leaf_flag, const ForestBufs& fb, cudaStream_t s,
-               int64_t* levels_out, std::string* err) {
+               int64_t* levels_out, std::string* err, const JobTable& jt, int roots_with_split) {
   auto fail = [&](cudaError_t e, const char* what) {
     if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
     return int(KNNG_E_CUDA);
@@ -346,9 +359,9 @@ int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t 
   init_perm<<<std::min<int64_t>(grid1(n * T), int64_t(sms) * 16), 256, 0, s>>>(perm, n, T);
   note_launch();
   NodeArr cur = node_arr(fb.node_a, fb.max_nodes), nxt = node_arr(fb.node_b, fb.max_nodes);
-  root_nodes<<<1, 32, 0, s>>>(cur, n, T, leaf, leaf_flag);
+  root_nodes<<<1, 64, 0, s>>>(cur, n, T, leaf, leaf_flag, jt, roots_with_split);
   note_launch();
-  int64_t cnt = n > leaf ? T : 0;
+  int64_t cnt = int64_t(T) * roots_with_split;
   int level = 0;
   int64_t host_i64[2];
   while (cnt > 0) {
@@ -365,7 +378,7 @@ int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t 
       }
       rep_dev = fb.replay_dev + 6 * lvl_off[level];
     }
-    pick_pivots<<<grid1(cnt), 256, 0, s>>>(cur, int(cnt), n, seed, level, perm, rep_dev, fb.child_cnt, fb.err);
+    pick_pivots<<<grid1(cnt), 256, 0, s>>>(cur, int(cnt), n, seed, level, perm, rep_dev, fb.child_cnt, fb.err, jt);
     note_launch();
     if ((e = exclusive_scan_i32(fb.child_cnt, fb.tile_off, cnt, fb.dev_i64, fb.scan_tmp, s))) return fail(e, "tile scan");
     if ((e = cudaMemcpyAsync(host_i64, fb.dev_i64, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "tile count");

@@ -210,17 +210,25 @@ __device__ int32_t dot_rows(const int8_t* a, const int8_t* b, int d) {
 // pool is (candidates by id asc) + xorshift32 fills with exact dots; sorted by
 // score (stable here), copied skipping adjacent equal ids, padded with random
 // ids of score INT32_MIN.  src/main.cpp:271-312.  One thread per row.
-__global__ void init_fixup(const int8_t* __restrict__ codes, int d, int64_t n, int K, uint32_t seed,
+__global__ void init_fixup(const int8_t* __restrict__ codes, int d, int64_t n_total, int K, uint32_t seed,
                            const int32_t* __restrict__ fix_rows, int64_t nfix, int32_t* __restrict__ ids,
-                           int32_t* __restrict__ scores) {
+                           int32_t* __restrict__ scores, JobTable jt) {
   const int64_t f = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (f >= nfix) return;
-  const int64_t i = fix_rows[f];
+  (void)n_total;
+  const int64_t gi = fix_rows[f];
+  // random ids are drawn job-locally (state seed + local row, ids modulo the
+  // job's n) exactly as a build of that job alone draws them
+  const int b = job_of(jt, gi);
+  const int64_t base = jt.off[b], n = jt.n[b], i = gi - base;
+  ids += base * K;
+  scores += base * K;
+  codes += base * int64_t(d);
   int32_t pid[kMaxK], psc[kMaxK];
   int c = 0;
   for (int k = 0; k < K; ++k)
     if (ids[i * K + k] >= 0) {
-      pid[c] = ids[i * K + k];
+      pid[c] = int32_t(ids[i * K + k] - base);  // job-local while the pool is built
       psc[c] = scores[i * K + k];
       ++c;
     }
@@ -262,7 +270,7 @@ __global__ void init_fixup(const int8_t* __restrict__ codes, int d, int64_t n, i
   int added = 0, last = -1;
   for (int p = 0; p < c && added < K; ++p)
     if (pid[p] != last) {
-      ids[i * K + added] = pid[p];
+      ids[i * K + added] = int32_t(pid[p] + base);
       scores[i * K + added] = psc[p];
       last = pid[p];
       ++added;
@@ -271,7 +279,7 @@ __global__ void init_fixup(const int8_t* __restrict__ codes, int d, int64_t n, i
     rs = xorshift32(rs);
     const int64_t r = int64_t(uint64_t(rs) % uint64_t(n));
     if (r != i || --budget <= 0) {
-      ids[i * K + added] = int32_t(r != i ? r : (i + 1) % n);
+      ids[i * K + added] = int32_t(base + (r != i ? r : (i + 1) % n));
       scores[i * K + added] = kScoreMinI;
       ++added;
     }
@@ -280,7 +288,7 @@ __global__ void init_fixup(const int8_t* __restrict__ codes, int d, int64_t n, i
 
 __global__ void export_kernel(const int32_t* __restrict__ ids, const int32_t* __restrict__ scores, int64_t n,
                               int K, int k_eval, const int32_t* __restrict__ id_map, int32_t* __restrict__ knns,
-                              float* __restrict__ dists) {
+                              float* __restrict__ dists, JobTable jt) {
   const int64_t tot = n * k_eval;
   for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < tot; q += int64_t(gridDim.x) * blockDim.x) {
     const int64_t i = q / k_eval;
@@ -288,6 +296,7 @@ __global__ void export_kernel(const int32_t* __restrict__ ids, const int32_t* __
     int32_t id = ids[i * K + k];
     const int32_t sc = scores[i * K + k];
     if (id_map) id = id_map[id];
+    if (jt.count > 1) id -= jt.off[job_of(jt, i)];
     const int64_t o = i * k_eval + (k_eval - 1 - k);
     knns[o] = id + 1;
     dists[o] = float(sc);
@@ -309,7 +318,7 @@ size_t init_bytes(int64_t n, int T, int leaf) {
 
 int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint32_t seed, const int32_t* perm,
              const uint8_t* leaf_flag, int32_t* ids, int32_t* scores, const InitBufs& ib, cudaStream_t s,
-             int64_t* leaves_out, std::string* err) {
+             int64_t* leaves_out, std::string* err, const JobTable& jt) {
   (void)leaf;
   auto fail = [&](cudaError_t e, const char* what) {
     if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
@@ -348,7 +357,7 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
   if ((e = cudaMemcpyAsync(&nfix, ib.dev_i64 + 1, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "fix count");
   if ((e = cudaStreamSynchronize(s))) return fail(e, "init merge");
   if (nfix > 0) {
-    init_fixup<<<grid1(nfix, 64), 64, 0, s>>>(codes, d, n, K, seed, ib.fix_rows, nfix, ids, scores);
+    init_fixup<<<grid1(nfix, 64), 64, 0, s>>>(codes, d, n, K, seed, ib.fix_rows, nfix, ids, scores, jt);
     note_launch();
     if ((e = cudaGetLastError())) return fail(e, "init fixup");
   }
@@ -356,11 +365,12 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
 }
 
 cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, int K, int k_eval,
-                          const int32_t* id_map, int32_t* knns, float* dists, cudaStream_t s) {
+                          const int32_t* id_map, int32_t* knns, float* dists, cudaStream_t s, const JobTable* jt) {
   const int64_t tot = n * k_eval;
   if (tot <= 0) return cudaSuccess;
+  const JobTable none{};
   export_kernel<<<unsigned(std::min<int64_t>(grid1(tot), 4096)), 256, 0, s>>>(ids, scores, n, K, k_eval, id_map,
-                                                                               knns, dists);
+                                                                               knns, dists, jt ? *jt : none);
   note_launch();
   return cudaGetLastError();
 }

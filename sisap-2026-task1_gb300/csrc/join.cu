@@ -36,7 +36,8 @@
 //   B  two-hop ids: warp per neighbour row (K contiguous ids), insert each,
 //      record its slot per j and the first j per slot (atomicMin)
 //   C  Hamming once per distinct id (the first occurrence of an id appends
-//      its slot to the distinct list during B):
+//      its slot to the distinct list during B); CB candidates in flight per
+//      8-lane group (the autotuned candidate block):
 //      8 lanes per candidate, one 16-byte sketch chunk per lane (128-byte
 //      rows = one line per candidate), warp __popc
 //   D  histogram of h over all occurrences, threshold h_t (warp scan)
@@ -134,11 +135,13 @@ __device__ __forceinline__ int table_insert(int32_t* key, uint32_t mask, int32_t
   return -1;
 }
 
-__global__ void __launch_bounds__(kThreads, 4) join_kernel(
+template <int CB, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     const int8_t* __restrict__ codes, const uint64_t* __restrict__ sketch, int64_t n, int d, int K, int R,
     const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out, int32_t* scores_out,
-    const int32_t* __restrict__ row_order, unsigned long long* __restrict__ counters) {
+    const int32_t* __restrict__ row_order, unsigned long long* __restrict__ counters, JobTable jt, JoinCtl ctl) {
   extern __shared__ __align__(16) unsigned char smem[];
+  if (ctl.all_done && *reinterpret_cast<volatile int*>(ctl.all_done)) return;
   const JoinSmem L = join_smem(K, R, d);
   uint4* my_code = reinterpret_cast<uint4*>(smem + L.o_code);
   uint4* my_sk = reinterpret_cast<uint4*>(smem + L.o_sk);
@@ -162,9 +165,23 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
   const uint32_t mask = uint32_t(L.HT - 1);
   const bool inplace = ids_out == ids_in;
   unsigned long long my_updates = 0, my_cands = 0, my_dots = 0;
+  int run_job = -1;                 // per-job update count kept by warp 0 lane 0
+  unsigned long long run_upd = 0;
 
   for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
     const int64_t i = row_order ? int64_t(row_order[r]) : r;
+    int job = 0;
+    if (ctl.job_done) {
+      job = job_of(jt, i);
+      if (ctl.job_done[job]) {  // stopped job: its rows pass through unchanged
+        if (!inplace)
+          for (int k = tid; k < K; k += kThreads) {
+            ids_out[i * K + k] = ids_in[i * K + k];
+            scores_out[i * K + k] = scores_in[i * K + k];
+          }
+        continue;
+      }
+    }
     // ---- A
     for (int k = tid; k < K; k += kThreads) {
       pool_id[k] = ids_in[i * K + k];
@@ -232,12 +249,12 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
     const int nu = s_nu;
     {
       const uint4 mine = sub < sk_chunks ? my_sk[sub] : make_uint4(0, 0, 0, 0);
-      for (int wbase = warp * 4; wbase < nu; wbase += 4 * kGroups) {
+      for (int wbase = warp * 4; wbase < nu; wbase += CB * kGroups) {
         const int base = wbase + slot8;
-        uint4 v[4];
-        int sl[4];
+        uint4 v[CB];
+        int sl[CB];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < CB; ++u) {
           const int q = base + u * kGroups;
           sl[u] = q < nu ? int(ulist[q]) : -1;
           v[u] = make_uint4(0, 0, 0, 0);
@@ -247,7 +264,7 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
           }
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < CB; ++u) {
           int pc = (sl[u] >= 0 && sub < sk_chunks) ? popc_u4(v[u], mine) : 0;
           pc += __shfl_xor_sync(0xffffffffu, pc, 1);
           pc += __shfl_xor_sync(0xffffffffu, pc, 2);
@@ -445,6 +462,14 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
       }
       for (int o = 16; o > 0; o >>= 1) changed += __shfl_xor_sync(full, changed, o);
       my_updates += unsigned(changed);
+      if (ctl.job_upd && lane == 0) {
+        if (job != run_job) {
+          if (run_job >= 0 && run_upd) atomicAdd(ctl.job_upd + run_job, run_upd);
+          run_job = job;
+          run_upd = 0;
+        }
+        run_upd += unsigned(changed);
+      }
     }
     __syncthreads();
   }
@@ -452,6 +477,36 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
     atomicAdd(counters + 0, my_updates);
     atomicAdd(counters + 1, my_cands);
     atomicAdd(counters + 2, my_dots);
+    if (ctl.job_upd && run_job >= 0 && run_upd) atomicAdd(ctl.job_upd + run_job, run_upd);
+  }
+}
+
+// Per-job early stop after an iteration, src/main.cpp:432-439 in float
+// arithmetic: rate = float(updates) / float(n * K); a job stops when
+// rate < stop or (iter > 0 and prev - rate < diff).  When every job has
+// stopped, all_done is set and final_buf records the buffer that holds the
+// final graphs; later iterations of the launch sequence then do nothing.
+__global__ void stop_check_kernel(JobTable jt, JoinCtl ctl, int K, int iter, int out_buf, float stop_rate,
+                                  float diff_tol) {
+  if (*ctl.all_done) return;
+  int all = 1;
+  for (int b = threadIdx.x; b < jt.count; b += blockDim.x) {
+    if (!ctl.job_done[b]) {
+      const unsigned long long upd = ctl.job_upd[b];
+      ctl.upd_log[int64_t(iter) * jt.count + b] = (long long)upd;
+      const float rate = float(upd) / float((unsigned long long)jt.n[b] * (unsigned long long)K);
+      const bool stop = rate < stop_rate || (iter > 0 && (ctl.job_prev[b] - rate) < diff_tol);
+      ctl.job_prev[b] = rate;
+      ctl.job_iters[b] = iter + 1;
+      ctl.job_upd[b] = 0;
+      if (stop) ctl.job_done[b] = 1;
+      else all = 0;
+    }
+  }
+  all = __syncthreads_and(all);
+  if (threadIdx.x == 0) {
+    *ctl.final_buf = out_buf;
+    if (all) *ctl.all_done = 1;
   }
 }
 
@@ -459,17 +514,49 @@ __global__ void __launch_bounds__(kThreads, 4) join_kernel(
 
 size_t join_smem_bytes(int K, int R, int d) { return join_smem(K, R, d).bytes; }
 
+template <int CB, int MINB>
+int max_ctas(size_t smem) {
+  if (cudaFuncSetAttribute(join_kernel<CB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) !=
+      cudaSuccess)
+    return 1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, join_kernel<CB, MINB>, kThreads, smem) != cudaSuccess)
+    return 1;
+  return per_sm < 1 ? 1 : per_sm;
+}
+
+int join_max_ctas_per_sm(int K, int R, int d) { return max_ctas<4, 4>(join_smem(K, R, d).bytes); }
+
+cudaError_t launch_stop_check(const JobTable& jt, const JoinCtl& ctl, int K, int iter, int out_buf, float stop_rate,
+                              float diff_tol, cudaStream_t s) {
+  stop_check_kernel<<<1, 256, 0, s>>>(jt, ctl, K, iter, out_buf, stop_rate, diff_tol);
+  note_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, int d, int K, int R,
                         const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out, int32_t* scores_out,
-                        const int32_t* row_order, unsigned long long* counters, int num_sms, cudaStream_t s) {
+                        const int32_t* row_order, unsigned long long* counters, int num_sms, cudaStream_t s,
+                        const JobTable* jt, const JoinCtl* ctl, int ctas_per_sm, int cblock) {
   const size_t smem = join_smem(K, R, d).bytes;
-  KNNG_CUDA_TRY(cudaFuncSetAttribute(join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  int per_sm = 0;
-  KNNG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, join_kernel, kThreads, smem));
-  if (per_sm < 1) per_sm = 1;
-  const int64_t blocks = std::min<int64_t>(n, int64_t(num_sms) * per_sm);
-  join_kernel<<<unsigned(blocks), kThreads, smem, s>>>(codes, sketch, n, d, K, R, ids_in, scores_in, ids_out,
-                                                       scores_out, row_order, counters);
+  const JobTable no_jobs{};
+  const JoinCtl no_ctl{};
+  auto go = [&](auto kern, int max_per_sm) {
+    const int64_t blocks = std::min<int64_t>(n, int64_t(num_sms) * max_per_sm);
+    kern<<<unsigned(blocks), kThreads, smem, s>>>(codes, sketch, n, d, K, R, ids_in, scores_in, ids_out, scores_out,
+                                                  row_order, counters, jt ? *jt : no_jobs, ctl ? *ctl : no_ctl);
+  };
+  // ctas_per_sm 3: up to 85 registers per thread (no spills), 3 resident CTAs;
+  // otherwise 64 registers, 4 resident CTAs
+  if (ctas_per_sm == 3) {
+    if (cblock == 2) go(join_kernel<2, 3>, max_ctas<2, 3>(smem));
+    else if (cblock == 8) go(join_kernel<8, 3>, max_ctas<8, 3>(smem));
+    else go(join_kernel<4, 3>, max_ctas<4, 3>(smem));
+  } else {
+    if (cblock == 2) go(join_kernel<2, 4>, max_ctas<2, 4>(smem));
+    else if (cblock == 8) go(join_kernel<8, 4>, max_ctas<8, 4>(smem));
+    else go(join_kernel<4, 4>, max_ctas<4, 4>(smem));
+  }
   note_launch();
   return cudaGetLastError();
 }

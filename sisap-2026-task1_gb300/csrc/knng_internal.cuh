@@ -24,6 +24,27 @@ inline bool dim_ok(int d) { return d >= 128 && d <= kMaxDim && d % 128 == 0; }
 int64_t launches();
 void note_launch(int k = 1);
 
+// A batch of independent jobs laid out back to back: job b owns global rows
+// [off[b], off[b] + n[b]) of an N-row problem (N = sum n).  Per-tree arrays are
+// tree-major, [T][N], so tree t of job b is the range t*N + off[b] ... and a
+// single build is the batch of one job (off = {0}, n = {N}).  Device copies of
+// off/n are read by the kernels that need a row's job (pivot identity, random
+// fills, per-job early stop, export of job-local ids).
+struct JobTable {
+  int count = 0;
+  const int32_t* off = nullptr;  // device, [count], ascending
+  const int32_t* n = nullptr;    // device, [count]
+};
+
+__device__ __forceinline__ int job_of(const JobTable& jt, int64_t row) {
+  int lo = 0, hi = jt.count - 1;  // largest b with off[b] <= row
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jt.off[mid] <= row) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 // ---- quantize.cu ----
 cudaError_t launch_quantize(const float* x, int64_t n, int d, int quant_mode, int8_t* codes,
                             uint64_t* sketch, cudaStream_t s);
@@ -55,7 +76,9 @@ struct ForestBufs {
 size_t forest_bytes(int64_t n, int T, int leaf, int64_t* max_nodes, int64_t* max_tiles);
 int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t seed,
                const int32_t* replay_host, int64_t n_replay, int32_t* perm, uint8_t* leaf_flag,
-               const ForestBufs& fb, cudaStream_t s, int64_t* levels_out, std::string* err);
+               const ForestBufs& fb, cudaStream_t s, int64_t* levels_out, std::string* err,
+               const JobTable& jt, int roots_with_split);
+// roots_with_split = number of jobs with n[b] > leaf (their T roots are split)
 
 // ---- init.cu ----
 struct InitBufs {
@@ -71,18 +94,42 @@ struct InitBufs {
 size_t init_bytes(int64_t n, int T, int leaf);
 int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint32_t seed,
              const int32_t* perm, const uint8_t* leaf_flag, int32_t* ids, int32_t* scores,
-             const InitBufs& ib, cudaStream_t s, int64_t* leaves_out, std::string* err);
+             const InitBufs& ib, cudaStream_t s, int64_t* leaves_out, std::string* err,
+             const JobTable& jt);
 
 // ---- join.cu ----
+// Per-batch NN-Descent control block in device memory.
+struct JoinCtl {
+  unsigned long long* counters;   // [3]: updates, distinct sketch candidates, reranked rows
+  unsigned long long* job_upd;    // [count]: updates of this iteration per job
+  int* job_done;                  // [count]: job stopped (its rows pass through)
+  float* job_prev;                // [count]: previous iteration's update rate
+  int* job_iters;                 // [count]: iterations run per job
+  int* all_done;                  // [1]
+  int* final_buf;                 // [1]: buffer index holding every job's final graph
+  long long* upd_log;             // [max_iter][count]: updates per iteration per job
+};
 cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, int d, int K, int R,
                         const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out,
                         int32_t* scores_out, const int32_t* row_order, unsigned long long* counters,
-                        int num_sms, cudaStream_t s);
-// counters[0] += updates, counters[1] += sketch candidates, counters[2] += reranked rows
+                        int num_sms, cudaStream_t s, const JobTable* jt = nullptr,
+                        const JoinCtl* ctl = nullptr, int ctas_per_sm = 0, int cblock = 4);
+// ctas_per_sm: 4 (64 registers per thread) or 3 (up to 85, no spills);
+// cblock: sketch candidates in flight per 8-lane group in the Hamming stage
+// (2, 4 or 8).  Both are chosen by the autotuner.
+// counters[0] += updates, counters[1] += distinct sketch candidates, counters[2] += reranked rows.
+// With jt/ctl: rows of stopped jobs are copied through (when out != in) and
+// per-job updates are added to ctl->job_upd; if ctl->all_done is set the launch
+// does nothing.
+cudaError_t launch_stop_check(const JobTable& jt, const JoinCtl& ctl, int K, int iter, int out_buf,
+                              float stop_rate, float diff_tol, cudaStream_t s);
+int join_max_ctas_per_sm(int K, int R, int d);
 
 // ---- export (init.cu) ----
 cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, int K, int k_eval,
-                          const int32_t* id_map, int32_t* knns, float* dists, cudaStream_t s);
+                          const int32_t* id_map, int32_t* knns, float* dists, cudaStream_t s,
+                          const JobTable* jt = nullptr);
+// With jt, ids are written job-local (id - off[job] + 1).
 
 }  // namespace knng
 

@@ -111,8 +111,16 @@ extern "C" int knng_init_graph_noalloc(const int8_t* codes_dev, int64_t n, int d
   InitBufs ib{};
   carve_init(static_cast<char*>(base), n, num_trees, &ib);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // one job covering all rows; its offset/size words live at the end of the scratch
+  int32_t* jt_dev = reinterpret_cast<int32_t*>(ib.dev_i64 + 2);
+  const int32_t jt_host[2] = {0, int32_t(n)};
+  if (cudaMemcpyAsync(jt_dev, jt_host, sizeof(jt_host), cudaMemcpyHostToDevice, s) != cudaSuccess) return KNNG_E_CUDA;
+  JobTable jt;
+  jt.count = 1;
+  jt.off = jt_dev;
+  jt.n = jt_dev + 1;
   st = run_init(codes_dev, n, d, num_trees, leaf_size, k_build, seed, perm_dev, leaf_flag_dev, ids_dev, scores_dev,
-                ib, s, nullptr, nullptr);
+                ib, s, nullptr, nullptr, jt);
   if (st) return st;
   return cudaStreamSynchronize(s) == cudaSuccess ? KNNG_OK : KNNG_E_CUDA;
 }

@@ -36,7 +36,8 @@ class Params(C.Structure):
         ("k_build", C.c_int), ("k_eval", C.c_int), ("num_trees", C.c_int), ("rerank_mult", C.c_int),
         ("leaf_size", C.c_int), ("max_iterations", C.c_int), ("early_stop_rate", C.c_float),
         ("rate_diff_tol", C.c_float), ("quant_mode", C.c_int), ("join_mode", C.c_int),
-        ("row_order", C.c_int), ("seed", C.c_uint32), ("device", C.c_int),
+        ("row_order", C.c_int), ("seed", C.c_uint32), ("device", C.c_int), ("autotune", C.c_int),
+        ("use_graph", C.c_int),
     ]
 
 
@@ -46,7 +47,8 @@ class Stats(C.Structure):
         ("export_s", C.c_double), ("build_s", C.c_double), ("total_s", C.c_double), ("iterations", C.c_int),
         ("updates", C.c_int64 * 64), ("forest_levels", C.c_int64), ("leaves", C.c_int64),
         ("device_s", C.c_double), ("join_ms", C.c_double * 64), ("join_candidates", C.c_int64 * 64),
-        ("join_dots", C.c_int64 * 64), ("kernel_launches", C.c_int64),
+        ("join_dots", C.c_int64 * 64), ("kernel_launches", C.c_int64), ("join_ctas_per_sm", C.c_int),
+        ("join_cblock", C.c_int), ("graph_used", C.c_int),
     ]
 
     def as_dict(self):
@@ -57,7 +59,7 @@ class Stats(C.Structure):
         return d
 
 
-EXPORTS = ["knng_default_params", "knng_create", "knng_destroy", "knng_build", "knng_status_string",
+EXPORTS = ["knng_default_params", "knng_create", "knng_destroy", "knng_build", "knng_build_batch", "knng_status_string",
            "knng_last_error", "knng_quantize", "knng_forest", "knng_init_graph", "knng_join_iter", "knng_export",
            "knng_init_graph_noalloc"]
 
@@ -78,6 +80,7 @@ def lib():
         L.knng_destroy.argtypes = [V]
         L.knng_destroy.restype = None
         L.knng_build.argtypes = [V, V, I64, C.c_int, C.c_int, V, V, C.c_int, P(Stats)]
+        L.knng_build_batch.argtypes = [V, P(Job), C.c_int, P(Stats)]
         L.knng_status_string.argtypes = [C.c_int]
         L.knng_status_string.restype = C.c_char_p
         L.knng_last_error.argtypes = [V]
@@ -126,6 +129,14 @@ def _stream_ptr(stream):
     if stream is None:
         return None
     return C.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+
+
+class Job(C.Structure):
+    _fields_ = [
+        ("rows", C.c_void_p), ("n", C.c_int64), ("d", C.c_int), ("rows_on_device", C.c_int),
+        ("knns", C.c_void_p), ("dists", C.c_void_p), ("out_on_device", C.c_int), ("status", C.c_int),
+        ("iterations", C.c_int),
+    ]
 
 
 class Context:
@@ -187,6 +198,36 @@ class Context:
         self._check(lib().knng_build(self.h, _ptr(rows), n, d, int(on_dev), _ptr(knns), _ptr(dists), out_dev,
                                      C.byref(st)))
         return knns, dists, st
+
+    def build_batch(self, rows_list, stats: Stats | None = None):
+        """Batched build of independent datasets (numpy or torch CUDA, any n and d).
+
+        Returns [(knns, dists, iterations), ...] in input order; outputs follow
+        each input's kind (numpy in -> numpy out, CUDA tensor in -> CUDA tensors)."""
+        st = stats or Stats()
+        jobs = (Job * len(rows_list))()
+        outs = []
+        keep = []
+        k_eval = self.prm.k_eval
+        for b, rows in enumerate(rows_list):
+            n, d = rows.shape
+            if isinstance(rows, np.ndarray):
+                rows = np.ascontiguousarray(rows, dtype=np.float32)
+                knns = np.empty((n, k_eval), np.int32)
+                dists = np.empty((n, k_eval), np.float32)
+                on_dev = 0
+            else:
+                import torch
+
+                on_dev = int(rows.is_cuda)
+                knns = torch.empty((n, k_eval), dtype=torch.int32, device=rows.device)
+                dists = torch.empty((n, k_eval), dtype=torch.float32, device=rows.device)
+            keep.append(rows)
+            jobs[b] = Job(_ptr(rows), n, d, on_dev, _ptr(knns), _ptr(dists), on_dev, 0, 0)
+            outs.append((knns, dists))
+        _ready(*[r for r in keep if not isinstance(r, np.ndarray)])
+        self._check(lib().knng_build_batch(self.h, jobs, len(rows_list), C.byref(st)))
+        return [(k, dd, jobs[b].iterations) for b, (k, dd) in enumerate(outs)], st
 
     # -- stages (torch CUDA tensors) --
     def forest(self, codes, replay=None, perm=None, leaf_flag=None):
