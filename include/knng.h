@@ -137,6 +137,52 @@ int knng_build(knng_ctx* ctx, const void* rows, int64_t n, int d, int rows_on_de
  * the groups. */
 int knng_build_batch(knng_ctx* ctx, knng_job* jobs, int count, knng_stats* stats);
 
+/* ---- serving loop (no counterpart in the reference) ----
+ * A server accepts build jobs as they arrive, admits them by device-memory
+ * footprint against mem_budget_gb, and runs whatever fits as a batch on each of
+ * `slots` worker streams, so jobs that arrive while others are on the GPU start
+ * as soon as a slot and memory free up and overlap on the device.  The job's
+ * rows and output buffers must stay valid until its ticket is done.  Each
+ * result is bit-identical to knng_build of the job alone. */
+typedef struct knng_server knng_server;
+
+typedef struct knng_server_params {
+  knng_params build;     /* build parameters of every job */
+  int slots;             /* concurrent batches (worker streams), default 3 */
+  double mem_budget_gb;  /* device memory the running batches may use, default 180 */
+  int max_batch_jobs;    /* jobs per batch, default 64 */
+} knng_server_params;
+
+typedef struct knng_result {
+  int status;            /* KNNG_OK, KNNG_E_ADMIT (larger than the budget), or a build error */
+  int iterations;        /* NN-Descent iterations of the job */
+  int batch_jobs;        /* size of the batch it ran in */
+  double queued_s;       /* submit -> batch start */
+  double run_s;          /* batch start -> done */
+  double latency_s;      /* submit -> done */
+} knng_result;
+
+void knng_server_default_params(knng_server_params* p);
+int knng_server_create(knng_server** out, const knng_server_params* p);
+/* Queue one job (the descriptor is copied); *ticket identifies it. */
+int knng_submit(knng_server* sv, const knng_job* job, uint64_t* ticket);
+/* KNNG_OK with *r filled when done, KNNG_E_BUSY while queued or running. */
+int knng_poll(knng_server* sv, uint64_t ticket, knng_result* r);
+/* Block until done or timeout_s elapsed (KNNG_E_TIMEOUT). */
+int knng_wait(knng_server* sv, uint64_t ticket, double timeout_s, knng_result* r);
+/* Forget a finished ticket. */
+int knng_release(knng_server* sv, uint64_t ticket);
+/* Stop the workers after their running batches; queued jobs are dropped. */
+void knng_server_destroy(knng_server* sv);
+
+/* Device bytes a build of n rows of dimension d needs with parameters p
+ * (NULL = defaults): the admission estimate of the serving loop. */
+int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on_device);
+
+/* Return all of the context's device buffers to the stream-ordered pool
+ * (kept for reuse otherwise). */
+int knng_trim(knng_ctx* ctx);
+
 /* Text for a status code, and the last detailed error message of ctx. */
 const char* knng_status_string(int status);
 const char* knng_last_error(const knng_ctx* ctx);

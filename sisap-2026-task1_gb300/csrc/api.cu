@@ -34,20 +34,24 @@ using namespace knng;
 
 constexpr int kMaxIterEvents = 2 * 64 + 2;
 
+// A context-owned device buffer, allocated and freed in the order of the
+// context's stream (the device's stream-ordered pool), so growing or trimming
+// one context never synchronises the device under other contexts' work.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t s = nullptr;
   cudaError_t ensure(size_t want) {
     if (want <= bytes) return cudaSuccess;
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
     p = nullptr;
     bytes = 0;
-    cudaError_t e = cudaMalloc(&p, want);
+    cudaError_t e = cudaMallocAsync(&p, want, s);
     if (e == cudaSuccess) bytes = want;
     return e;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
     p = nullptr;
     bytes = 0;
   }
@@ -72,6 +76,9 @@ struct knng_ctx {
   std::vector<uintptr_t> join_graph_key;
   // autotuned join configuration per (d, log2 rows): (ctas_per_sm, cblock)
   std::map<std::pair<int, int>, std::pair<int, int>> tuned;
+  std::vector<DevBuf*> buffers() {
+    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs};
+  }
 };
 
 namespace {
@@ -538,6 +545,7 @@ int knng_create(knng_ctx** out, const knng_params* p) {
       knng_destroy(c);
       return KNNG_E_CUDA;
     }
+  for (DevBuf* b : c->buffers()) b->s = c->stream;
   *out = c;
   return KNNG_OK;
 }
@@ -547,9 +555,8 @@ void knng_destroy(knng_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->join_graph) cudaGraphExecDestroy(c->join_graph);
-  for (DevBuf* b : {&c->codes, &c->sketch, &c->graph, &c->perm, &c->leaf_flag, &c->scratch, &c->staging,
-                    &c->outbuf, &c->scalars, &c->jobs})
-    b->release();
+  for (DevBuf* b : c->buffers()) b->release();
+  if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& ev : c->itev)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : c->ev)
@@ -646,6 +653,34 @@ int knng_build(knng_ctx* c, const void* rows, int64_t n, int d, int rows_on_devi
   BJob j{rows, n, rows_on_device, knns, dists, out_on_device, 0};
   knng_stats local{};
   return run_batch(c, &j, 1, d, stats ? *stats : local);
+}
+
+int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on_device) {
+  knng_params q;
+  if (p) q = *p; else knng_default_params(&q);
+  if (n < 1 || d < 1) return 0;
+  const int T = q.num_trees, K = q.k_build;
+  int64_t mn = 0, mt = 0;
+  const size_t f = forest_bytes(n, T, q.leaf_size, &mn, &mt);
+  const size_t in = init_bytes(n, T, q.leaf_size);
+  size_t b = size_t(n) * d + size_t(n) * (d / 64) * 8 + size_t(n) * K * 16 + size_t(T) * n * 5;
+  b += std::max(f, in) + 64 * 1024;
+  b += size_t(n) * q.k_eval * 8;                                   // export buffer
+  b += size_t(q.max_iterations + 1) * 64 * 8 + 4096;               // control block (per job, bounded)
+  if (!rows_on_device) b += size_t(2) * kStageRows * d * 4;        // host-input staging
+  return int64_t(b) + (int64_t(1) << 24);                          // pool rounding slack
+}
+
+int knng_trim(knng_ctx* c) {
+  if (!c) return KNNG_E_ARGS;
+  cudaSetDevice(c->device);
+  if (c->join_graph) {
+    cudaGraphExecDestroy(c->join_graph);
+    c->join_graph = nullptr;
+    c->join_graph_key.clear();
+  }
+  for (DevBuf* b : c->buffers()) b->release();
+  return KNNG_OK;
 }
 
 int knng_build_batch(knng_ctx* c, knng_job* jobs, int count, knng_stats* stats) {

@@ -61,7 +61,8 @@ class Stats(C.Structure):
 
 EXPORTS = ["knng_default_params", "knng_create", "knng_destroy", "knng_build", "knng_build_batch", "knng_status_string",
            "knng_last_error", "knng_quantize", "knng_forest", "knng_init_graph", "knng_join_iter", "knng_export",
-           "knng_init_graph_noalloc"]
+           "knng_init_graph_noalloc", "knng_footprint_bytes", "knng_trim", "knng_server_default_params",
+           "knng_server_create", "knng_submit", "knng_poll", "knng_wait", "knng_release", "knng_server_destroy"]
 
 _lib = None
 
@@ -91,6 +92,18 @@ def lib():
         L.knng_join_iter.argtypes = [V, V, V, I64, C.c_int, V, V, V, V, P(I64)]
         L.knng_export.argtypes = [V, V, I64, C.c_int, C.c_int, V, V, V, V]
         L.knng_init_graph_noalloc.argtypes = [V, I64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32, V, V, V, V, V]
+        L.knng_footprint_bytes.argtypes = [P(Params), I64, C.c_int, C.c_int]
+        L.knng_footprint_bytes.restype = I64
+        L.knng_trim.argtypes = [V]
+        L.knng_server_default_params.argtypes = [P(ServerParams)]
+        L.knng_server_default_params.restype = None
+        L.knng_server_create.argtypes = [P(V), P(ServerParams)]
+        L.knng_submit.argtypes = [V, P(Job), P(C.c_uint64)]
+        L.knng_poll.argtypes = [V, C.c_uint64, P(Result)]
+        L.knng_wait.argtypes = [V, C.c_uint64, C.c_double, P(Result)]
+        L.knng_release.argtypes = [V, C.c_uint64]
+        L.knng_server_destroy.argtypes = [V]
+        L.knng_server_destroy.restype = None
         _lib = L
     return _lib
 
@@ -137,6 +150,80 @@ class Job(C.Structure):
         ("knns", C.c_void_p), ("dists", C.c_void_p), ("out_on_device", C.c_int), ("status", C.c_int),
         ("iterations", C.c_int),
     ]
+
+
+class ServerParams(C.Structure):
+    _fields_ = [("build", Params), ("slots", C.c_int), ("mem_budget_gb", C.c_double), ("max_batch_jobs", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("batch_jobs", C.c_int), ("queued_s", C.c_double),
+                ("run_s", C.c_double), ("latency_s", C.c_double)]
+
+
+class Server:
+    """The serving loop: submit builds as they arrive, wait on tickets."""
+
+    def __init__(self, slots=3, mem_budget_gb=180.0, max_batch_jobs=64, **build_kw):
+        sp = ServerParams()
+        lib().knng_server_default_params(C.byref(sp))
+        sp.build = params(**build_kw)
+        sp.slots, sp.mem_budget_gb, sp.max_batch_jobs = slots, mem_budget_gb, max_batch_jobs
+        self.k_eval = sp.build.k_eval
+        self.h = C.c_void_p()
+        st = lib().knng_server_create(C.byref(self.h), C.byref(sp))
+        if st != 0:
+            raise KnngError(st, "knng_server_create")
+        self.live = {}
+
+    def submit(self, rows):
+        """Queue a build of rows (numpy or torch CUDA float32); returns a ticket."""
+        n, d = rows.shape
+        if isinstance(rows, np.ndarray):
+            rows = np.ascontiguousarray(rows, dtype=np.float32)
+            knns, dists, dev = np.empty((n, self.k_eval), np.int32), np.empty((n, self.k_eval), np.float32), 0
+        else:
+            import torch
+
+            _ready(rows)
+            dev = int(rows.is_cuda)
+            knns = torch.empty((n, self.k_eval), dtype=torch.int32, device=rows.device)
+            dists = torch.empty((n, self.k_eval), dtype=torch.float32, device=rows.device)
+        job = Job(_ptr(rows), n, d, dev, _ptr(knns), _ptr(dists), dev, 0, 0)
+        t = C.c_uint64(0)
+        st = lib().knng_submit(self.h, C.byref(job), C.byref(t))
+        if st != 0:
+            raise KnngError(st, "knng_submit")
+        self.live[t.value] = (rows, knns, dists)
+        return t.value
+
+    def poll(self, ticket):
+        r = Result()
+        st = lib().knng_poll(self.h, ticket, C.byref(r))
+        return None if st == -8 else self._finish(ticket, st, r)
+
+    def wait(self, ticket, timeout_s=600.0):
+        r = Result()
+        st = lib().knng_wait(self.h, ticket, timeout_s, C.byref(r))
+        return self._finish(ticket, st, r)
+
+    def _finish(self, ticket, st, r):
+        if st != 0:
+            raise KnngError(st, "knng_wait/poll")
+        _, knns, dists = self.live.pop(ticket)
+        lib().knng_release(self.h, ticket)
+        return knns, dists, r
+
+    def close(self):
+        if self.h:
+            lib().knng_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Context:

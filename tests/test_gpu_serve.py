@@ -1,0 +1,95 @@
+"""The serving loop (knng_server): jobs submitted while others run are admitted
+by memory footprint, batched and overlapped on the device, and each result is
+the same as the job built alone (bit for bit: the batch keeps per-job pivots,
+fills and early stop, and the update is double-buffered)."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def knng_mod():
+    import torch
+
+    assert torch.cuda.is_available(), "the gpu tests need a CUDA device"
+    import knng
+
+    knng.lib()
+    return knng
+
+
+def test_served_results_equal_alone(knng_mod):
+    import torch
+
+    knng = knng_mod
+    specs = [(20000, 1024, 200), (3000, 1024, 30), (9000, 1024, 900), (500, 1024, 5), (15000, 1024, 150),
+             (7000, 1024, 70), (1200, 1024, 12), (30000, 1024, 300)]
+    xs = [synth.mixture(n, d, c, seed=300 + k) for k, (n, d, c) in enumerate(specs)]
+    with knng.Context() as ctx:
+        solo = [ctx.build(x)[:2] for x in xs]
+    with knng.Server(slots=2) as sv:
+        tickets = []
+        for k, x in enumerate(xs):  # staggered arrivals, half on the device
+            tickets.append(sv.submit(torch.from_numpy(x).cuda() if k % 2 else x))
+            time.sleep(0.01)
+        outs = [sv.wait(t) for t in tickets]
+    batched = 0
+    for (k, dd, r), (ks, ds) in zip(outs, solo):
+        assert r.status == 0 and r.latency_s >= r.run_s >= 0
+        batched += r.batch_jobs > 1
+        k = k.cpu().numpy() if hasattr(k, "cpu") else k
+        dd = dd.cpu().numpy() if hasattr(dd, "cpu") else dd
+        np.testing.assert_array_equal(k, ks)
+        np.testing.assert_array_equal(dd, ds)
+    assert batched > 0  # jobs that arrived while a batch ran were batched together
+
+
+def test_admission_by_footprint(knng_mod):
+    knng = knng_mod
+    big = synth.mixture(60000, 1024, 600, seed=9)
+    small = synth.mixture(2000, 1024, 20, seed=10)
+    budget_gb = 1.5 * knng.lib().knng_footprint_bytes(None, 2000, 1024, 0) / 1e9
+    with knng.Server(slots=1, mem_budget_gb=budget_gb) as sv:
+        tb = sv.submit(big)
+        ts = sv.submit(small)
+        _, _, rb = sv.wait(tb)
+        ks, ds, rs = sv.wait(ts)
+    assert rb.status == -4  # larger than the whole budget: refused
+    assert rs.status == 0 and ks.min() >= 1
+
+
+def test_poll_and_concurrent_submitters(knng_mod):
+    knng = knng_mod
+    xs = [synth.mixture(4000, 768, 40, seed=20 + k) for k in range(6)]
+    with knng.Context() as ctx:
+        solo = [ctx.build(x)[:2] for x in xs]
+    with knng.Server(slots=3) as sv:
+        tickets = [None] * len(xs)
+
+        def submit(k):
+            tickets[k] = sv.submit(xs[k])
+
+        ths = [threading.Thread(target=submit, args=(k,)) for k in range(len(xs))]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        done = {}
+        deadline = time.time() + 120
+        while len(done) < len(xs) and time.time() < deadline:
+            for k, t in enumerate(tickets):
+                if k not in done:
+                    r = sv.poll(t)
+                    if r is not None:
+                        done[k] = r
+            time.sleep(0.005)
+    assert len(done) == len(xs)
+    for k, (kn, dd, r) in done.items():
+        np.testing.assert_array_equal(kn, solo[k][0])
+        np.testing.assert_array_equal(dd, solo[k][1])
