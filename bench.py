@@ -203,7 +203,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    cfg = CONFIGS[args.config]
+    cfg = CONFIGS.get(args.config, CONFIGS["full"])
     times = []
     for k in range(args.warmup + args.steps):
         s, n = cpu_port_step(threads)
@@ -220,6 +220,122 @@ def run_reference(args):
         "e2e": {"value": v, "unit": "vectors/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference src/main.cpp needs libhdf5 and cannot run on this host; its restatement (oracle/knng_oracle.cpp, pinned bit-exact to the reference binary) runs with OpenMP",
     }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _job_specs(count, lo, hi, dims, seed):
+    """Seeded (n, d) of `count` jobs: n log-uniform in [lo, hi], d drawn from dims."""
+    import numpy as np
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.int64)
+    ds = rng.choice(np.asarray(dims), size=count)
+    return [(int(n), int(d)) for n, d in zip(ns, ds)]
+
+
+def run_batched(args):
+    """64 independent jobs (n log-uniform in [5k, 200k], d in {384, 768, 1024}):
+    one knng_build_batch call per step against the same jobs as 64 plain
+    knng_build calls.  value = batched jobs/s; every job's output is checked
+    bit-identical between the two."""
+    import numpy as np
+    import torch
+
+    import knng
+    import synth
+
+    dev = torch.device("cuda", 0)
+    specs = _job_specs(64, 5_000, 200_000, (384, 768, 1024), seed=4003)
+    xs = [synth.mixture_torch(n, d, max(1, n // 100), seed=4000 + j, device=dev) for j, (n, d) in enumerate(specs)]
+    torch.cuda.synchronize()
+    rows = sum(n for n, _ in specs)
+    with knng.Context() as ctx:
+        for _ in range(args.warmup):
+            res, _ = ctx.build_batch(xs)
+        bt = []
+        launches = 0
+        with ClockSampler(0) as clk:
+            for _ in range(args.steps):
+                st = knng.Stats()
+                res, st = ctx.build_batch(xs, st)
+                bt.append(st.device_s)
+                launches += st.kernel_launches
+        for x in xs[:2]:
+            ctx.build(x)  # warm the single-build path
+        seq = []
+        same = True
+        for _ in range(max(1, args.steps // 2)):
+            tot = 0.0
+            for j, x in enumerate(xs):
+                k, d_, st1 = ctx.build(x)
+                tot += st1.device_s
+                same &= bool(torch.equal(k, res[j][0]) and torch.equal(d_, res[j][1]))
+            seq.append(tot)
+    b_js = 64 / statistics.mean(bt)
+    s_js = 64 / statistics.mean(seq)
+    line = {"metric": "jobs/s (64 independent kNN-graph builds, batched)", "value": b_js, "unit": "jobs/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(bt),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8/int32",
+            "data": "synthetic (seeded Gaussian mixtures, one per job)",
+            "config": {"workload": "batched builds: 64 jobs, n log-uniform [5k, 200k], d in {384, 768, 1024}",
+                       "rows": rows, "l2": "inputs far larger than L2"},
+            "sequential_plain_jobs_per_s": s_js, "batched_over_sequential": b_js / s_js,
+            "identical_to_plain": same, "vectors_per_s": rows / statistics.mean(bt),
+            "clocks": clk.summary(), "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serving(args):
+    """Poisson arrivals (mean 4 jobs/s) of builds with n log-uniform in [10k, 2M],
+    d = 1024, rows resident in HBM; the server admits them by footprint against
+    180 GB and batches them continuously.  Reports jobs/s and p50/p99 latency
+    next to the same jobs built one after another."""
+    import numpy as np
+    import torch
+
+    import knng
+    import synth
+
+    dev = torch.device("cuda", 0)
+    count = args.serve_jobs
+    specs = _job_specs(count, 10_000, 2_000_000, (1024,), seed=5003)
+    xs = [synth.mixture_torch(n, d, max(1, n // 100), seed=5000 + j, device=dev) for j, (n, d) in enumerate(specs)]
+    torch.cuda.synchronize()
+    rng = np.random.Generator(np.random.PCG64(5))
+    gaps = rng.exponential(1.0 / 4.0, size=count)
+    with knng.Context() as ctx:  # warm-up + sequential reference
+        ctx.build(xs[0])
+        seq_s = 0.0
+        solo = {}
+        for j, x in enumerate(xs):
+            k, d_, st = ctx.build(x)
+            seq_s += st.device_s
+            if j < 4:
+                solo[j] = (k, d_)
+    with knng.Server(slots=args.slots, mem_budget_gb=180.0) as sv:
+        sv.wait(sv.submit(xs[0]))  # warm the workers
+        tickets = [None] * count
+        t0 = time.perf_counter()
+        with ClockSampler(0) as clk:
+            for j in range(count):
+                time.sleep(gaps[j])
+                tickets[j] = sv.submit(xs[j])
+            outs = [sv.wait(t, 1200.0) for t in tickets]
+            t_end = time.perf_counter()
+    lat = sorted(r.latency_s for _, _, r in outs)
+    same = all(torch.equal(outs[j][0], solo[j][0]) and torch.equal(outs[j][1], solo[j][1]) for j in solo)
+    arrive_span = float(np.sum(gaps))
+    line = {"metric": "jobs/s (serving, Poisson 4 jobs/s, n log-uniform [10k, 2M])", "value": count / (t_end - t0),
+            "unit": "jobs/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * (t_end - t0),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8/int32",
+            "data": "synthetic (seeded Gaussian mixtures, one per job)",
+            "config": {"workload": f"serving loop: {count} jobs, Poisson mean 4/s, d=1024, 180 GB budget",
+                       "slots": args.slots, "rows": int(sum(n for n, _ in specs)), "arrival_span_s": arrive_span},
+            "p50_latency_s": lat[len(lat) // 2], "p99_latency_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+            "mean_batch_jobs": float(np.mean([r.batch_jobs for _, _, r in outs])),
+            "sequential_plain_jobs_per_s": count / seq_s, "identical_to_plain": same, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -339,7 +455,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--config", default="full", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="full", choices=sorted(CONFIGS) + ["batched", "serving"])
+    ap.add_argument("--serve-jobs", type=int, default=32)
+    ap.add_argument("--slots", type=int, default=3)
     ap.add_argument("--recall-rows", type=int, default=10_000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
@@ -350,6 +468,10 @@ def main():
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "batched":
+        return run_batched(args)
+    if args.config == "serving":
+        return run_serving(args)
     return run_gpu(args)
 
 
