@@ -33,11 +33,11 @@ def test_served_results_equal_alone(knng_mod):
     xs = [synth.mixture(n, d, c, seed=300 + k) for k, (n, d, c) in enumerate(specs)]
     with knng.Context() as ctx:
         solo = [ctx.build(x)[:2] for x in xs]
-    with knng.Server(slots=2) as sv:
-        tickets = []
-        for k, x in enumerate(xs):  # staggered arrivals, half on the device
-            tickets.append(sv.submit(torch.from_numpy(x).cuda() if k % 2 else x))
-            time.sleep(0.01)
+    dev_x = {k: torch.from_numpy(x).cuda() for k, x in enumerate(xs) if k % 2}
+    with knng.Server(slots=1) as sv:
+        # all arrive while the first build runs on the single slot: they are
+        # admitted together as the next batch; half the inputs are on the device
+        tickets = [sv.submit(dev_x.get(k, x)) for k, x in enumerate(xs)]
         outs = [sv.wait(t) for t in tickets]
     batched = 0
     for (k, dd, r), (ks, ds) in zip(outs, solo):
