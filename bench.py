@@ -198,6 +198,19 @@ def recall_parity(x_np, ref_knns, dev):
     return {"n": int(x.shape[0]), "reference_port": r_ref, "gpu": r_gpu, "gap_pt": 100 * (r_ref - r_gpu)}
 
 
+def committed_traffic():
+    """DRAM bytes (read + write) per working join launch of the full workload,
+    from the committed ncu summary; None when absent."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "join_kernel_dram_full_6.35M.md")) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -414,6 +427,9 @@ def run_gpu(args):
                 "ms_per_launch": sum(join_ms) / max(1, it)}
     if args.traffic_per_launch:
         roofline["traffic"] = args.traffic_per_launch
+    elif args.config == "full":
+        roofline["traffic"] = committed_traffic()
+        roofline["traffic_source"] = "profiles/join_kernel_dram_full_6.35M.md (ncu, mean of the 7 working launches)"
     # ---- recall on a seeded sample
     rec = recall_sample(x, knns, rows=args.recall_rows) if args.recall_rows > 0 and rank == 0 else None
     # ---- CPU baseline (rank 0, N=1 only)
