@@ -44,6 +44,7 @@ typedef enum knng_status {
 enum { KNNG_QUANT_TRUNC = 0, KNNG_QUANT_ROUND = 1 };
 enum { KNNG_JOIN_JACOBI = 0, KNNG_JOIN_INPLACE = 1 };
 enum { KNNG_ORDER_NATURAL = 0, KNNG_ORDER_LEAF = 1 };
+enum { KNNG_GRAM_DP4A = 0, KNNG_GRAM_TCGEN05 = 1 };
 
 /* Build parameters.  Defaults (knng_default_params) are the reference's
  * compile-time constants, src/main.cpp:19-29. */
@@ -63,6 +64,7 @@ typedef struct knng_params {
   int device;            /* CUDA device ordinal */
   int autotune;          /* 1: time the join configurations once per (d, size) */
   int use_graph;         /* 1: replay the NN-Descent phase as a CUDA graph */
+  int gram_mode;         /* leaf Gram: KNNG_GRAM_DP4A or KNNG_GRAM_TCGEN05 (bf16 tensor cores) */
 } knng_params;
 
 /* Per-build timings and convergence record (seconds, device-timed). */

@@ -109,6 +109,7 @@ int check_params(knng_ctx* c, const knng_params& p) {
   if (p.quant_mode != KNNG_QUANT_TRUNC && p.quant_mode != KNNG_QUANT_ROUND) return set_error(c, KNNG_E_ARGS, "bad quant_mode");
   if (p.join_mode != KNNG_JOIN_JACOBI && p.join_mode != KNNG_JOIN_INPLACE) return set_error(c, KNNG_E_ARGS, "bad join_mode");
   if (p.row_order != KNNG_ORDER_NATURAL && p.row_order != KNNG_ORDER_LEAF) return set_error(c, KNNG_E_ARGS, "bad row_order");
+  if (p.gram_mode != KNNG_GRAM_DP4A && p.gram_mode != KNNG_GRAM_TCGEN05) return set_error(c, KNNG_E_ARGS, "bad gram_mode");
   return KNNG_OK;
 }
 
@@ -362,7 +363,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     return st;
   cudaEventRecord(c->ev[2], str);
   if ((st = run_init(c->codes.as<int8_t>(), N, d, T, p.leaf_size, K, p.seed, c->perm.as<int32_t>(),
-                     c->leaf_flag.as<uint8_t>(), ids[0], scs[0], s.ib, str, &leaves, &c->last_error, jt)))
+                     c->leaf_flag.as<uint8_t>(), ids[0], scs[0], s.ib, str, &leaves, &c->last_error, jt, p.gram_mode)))
     return st;
   const int32_t* order = p.row_order == KNNG_ORDER_LEAF ? c->perm.as<int32_t>() : nullptr;
   const std::pair<int, int> cfg = autotune_join(c, N, d, ids, scs, order, tune_counters);
@@ -490,6 +491,7 @@ void knng_default_params(knng_params* p) {
   p->device = 0;
   p->autotune = 1;
   p->use_graph = 1;
+  p->gram_mode = 0;
 }
 
 const char* knng_status_string(int s) {
@@ -606,7 +608,7 @@ int knng_init_graph(knng_ctx* c, const int8_t* codes_dev, int64_t n, int d, cons
   JobTable jt;
   if ((st = single_job(c, n, &jt))) return st;
   st = run_init(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.k_build, c->prm.seed, perm_dev,
-                leaf_flag_dev, ids_dev, scores_dev, s.ib, c->stream, nullptr, &c->last_error, jt);
+                leaf_flag_dev, ids_dev, scores_dev, s.ib, c->stream, nullptr, &c->last_error, jt, c->prm.gram_mode);
   if (st) return st;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   return e ? cuda_fail(c, e, "init") : KNNG_OK;

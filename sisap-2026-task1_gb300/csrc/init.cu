@@ -318,7 +318,7 @@ size_t init_bytes(int64_t n, int T, int leaf) {
 
 int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint32_t seed, const int32_t* perm,
              const uint8_t* leaf_flag, int32_t* ids, int32_t* scores, const InitBufs& ib, cudaStream_t s,
-             int64_t* leaves_out, std::string* err, const JobTable& jt) {
+             int64_t* leaves_out, std::string* err, const JobTable& jt, int gram_mode) {
   (void)leaf;
   auto fail = [&](cudaError_t e, const char* what) {
     if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
@@ -343,19 +343,33 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
   leaf_fill<<<unsigned(std::min<int64_t>(grid1(nleaves), int64_t(sms) * 32)), 256, 0, s>>>(
       leaf_start, nleaves, tn, n, perm, ib.pos, ib.leaf_lo, ib.leaf_sz);
   note_launch();
-  const size_t smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
-  if ((e = cudaFuncSetAttribute(leaf_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))))
-    return fail(e, "gram smem");
-  leaf_gram<<<unsigned(std::min<int64_t>(nleaves, int64_t(sms) * 24)), kGramThreads, smem, s>>>(
-      codes, d, perm, leaf_start, nleaves, tn, ib.gram);
-  note_launch();
+  unsigned* gerr = reinterpret_cast<unsigned*>(ib.dev_i64 + 3);
+  if (gram_mode == 1) {
+    if ((e = cudaMemsetAsync(gerr, 0, sizeof(unsigned), s))) return fail(e, "gram flag");
+    if ((e = launch_leaf_gram_tc(codes, d, perm, leaf_start, nleaves, tn, ib.gram, gerr, sms, s)))
+      return fail(e, "tensor-core gram");
+  } else {
+    const size_t smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
+    if ((e = cudaFuncSetAttribute(leaf_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))))
+      return fail(e, "gram smem");
+    leaf_gram<<<unsigned(std::min<int64_t>(nleaves, int64_t(sms) * 24)), kGramThreads, smem, s>>>(
+        codes, d, perm, leaf_start, nleaves, tn, ib.gram);
+    note_launch();
+  }
   if ((e = cudaMemsetAsync(ib.dev_i64 + 1, 0, 8, s))) return fail(e, "fix count");
   init_merge<<<unsigned(std::min<int64_t>((n + 7) / 8, int64_t(sms) * 16)), 256, 0, s>>>(
       n, T, K, perm, ib.pos, ib.leaf_lo, ib.leaf_sz, ib.gram, ids, scores, ib.fix_rows, ib.dev_i64 + 1);
   note_launch();
   int64_t nfix = 0;
+  unsigned gflag = 0;
   if ((e = cudaMemcpyAsync(&nfix, ib.dev_i64 + 1, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "fix count");
+  if (gram_mode == 1 && (e = cudaMemcpyAsync(&gflag, gerr, sizeof(unsigned), cudaMemcpyDeviceToHost, s)))
+    return fail(e, "gram flag");
   if ((e = cudaStreamSynchronize(s))) return fail(e, "init merge");
+  if (gflag & kErrTimeout) {
+    if (err) *err = "tensor-core leaf Gram: an mbarrier wait timed out";
+    return KNNG_E_TIMEOUT;
+  }
   if (nfix > 0) {
     init_fixup<<<grid1(nfix, 64), 64, 0, s>>>(codes, d, n, K, seed, ib.fix_rows, nfix, ids, scores, jt);
     note_launch();

@@ -16,7 +16,7 @@ constexpr int kMaxLeaf = 64;     // leaf_size upper bound (64-wide Gram rows)
 constexpr int kScoreMinI = INT32_MIN;
 
 // Device-side error flag bits (written by kernels, read by the host).
-enum : unsigned { kErrReplay = 1u, kErrBounds = 2u };
+enum : unsigned { kErrReplay = 1u, kErrBounds = 2u, kErrTimeout = 4u };
 
 inline bool dim_ok(int d) { return d >= 128 && d <= kMaxDim && d % 128 == 0; }
 
@@ -95,7 +95,11 @@ size_t init_bytes(int64_t n, int T, int leaf);
 int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint32_t seed,
              const int32_t* perm, const uint8_t* leaf_flag, int32_t* ids, int32_t* scores,
              const InitBufs& ib, cudaStream_t s, int64_t* leaves_out, std::string* err,
-             const JobTable& jt);
+             const JobTable& jt, int gram_mode = 0);
+// gram_mode 0: dp4a leaf Gram (leaf_gram); 1: tcgen05 bf16 tensor-core Gram (leaf_gram_tc)
+cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm, const int32_t* leaf_start,
+                                int64_t nleaves, int64_t total, int32_t* gram, unsigned* err, int num_sms,
+                                cudaStream_t s);
 
 // ---- join.cu ----
 // Per-batch NN-Descent control block in device memory.
