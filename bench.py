@@ -39,6 +39,7 @@ CONFIGS = {
 }
 CPU_SAMPLE = (100_000, 1024, 1_000)  # bounded CPU sample (the 100k small config), ~10-30 s of CPU work
 METRIC = "vectors/s (kNN-graph build, recall@15-checked)"
+GRAM = {"dp4a": 0, "tc": 1}
 
 
 def load_peaks():
@@ -366,7 +367,7 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     x = synth.mixture_torch(n, d, centres, seed=1000 * 2 + rank, device=dev)
     torch.cuda.synchronize()
-    prm = knng.params(device=local)
+    prm = knng.params(device=local, gram_mode=GRAM[args.gram])
     ctx = knng.Context(prm)
     knns = torch.empty((n, prm.k_eval), dtype=torch.int32, device=dev)
     dists = torch.empty((n, prm.k_eval), dtype=torch.float32, device=dev)
@@ -450,6 +451,7 @@ def run_gpu(args):
             "config": {"workload": desc, "n": n, "d": d, "centres": centres, "k": prm.k_eval,
                        "k_build": K, "trees": prm.num_trees, "leaf": prm.leaf_size, "rerank": prm.rerank_mult,
                        "join": "jacobi" if prm.join_mode == 0 else "inplace",
+                       "leaf_gram": "tcgen05 bf16" if prm.gram_mode == 1 else "dp4a",
                        "l2": "inputs (n x d float32) far larger than L2; no flush",
                        "parallelism": f"replicas x{ws}"},
             "build_s": last.build_s, "step_s": last.device_s, "iterations": it,
@@ -472,6 +474,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--config", default="full", choices=sorted(CONFIGS) + ["batched", "serving"])
+    ap.add_argument("--gram", default="tc", choices=["tc", "dp4a"],
+                    help="leaf Gram: tcgen05 bf16 tensor cores or dp4a")
     ap.add_argument("--serve-jobs", type=int, default=32)
     ap.add_argument("--slots", type=int, default=3)
     ap.add_argument("--recall-rows", type=int, default=10_000)

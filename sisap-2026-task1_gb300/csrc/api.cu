@@ -491,7 +491,7 @@ void knng_default_params(knng_params* p) {
   p->device = 0;
   p->autotune = 1;
   p->use_graph = 1;
-  p->gram_mode = 0;
+  p->gram_mode = KNNG_GRAM_TCGEN05;
 }
 
 const char* knng_status_string(int s) {
