@@ -94,7 +94,7 @@ __host__ __device__ inline JoinSmem join_smem(int K, int R, int d) {
   s.o_key = o;     o = align16(o + size_t(s.HT) * 4);
   s.o_meta = o;    o = align16(o + size_t(s.HT) * 4);
   s.o_hist = o;    o = align16(o + size_t(kHBins) * 4);
-  s.o_ulist = o;   o = align16(o + size_t(s.KK) * 2);
+  s.o_ulist = o;   o = align16(o + size_t(s.KK + K) * 2);  // <= K starting-list + K*K candidate slots
   s.o_need = o;    o = align16(o + size_t(R) * 2);
   s.o_pkey = o;    o = align16(o + size_t(R) * 4);
   s.o_pid = o;     o = align16(o + size_t(R) * 4);

@@ -211,3 +211,38 @@ def test_export_bit_exact(torch_dev):
     k, dd = knng.export(torch.from_numpy(ids).to(dev), torch.from_numpy(np.ascontiguousarray(sc)).to(dev), 15)
     np.testing.assert_array_equal(k.cpu().numpy(), kr)
     np.testing.assert_array_equal(dd.cpu().numpy(), dr)
+
+
+@pytest.mark.parametrize("k,mult", [(50, 8), (20, 3)])
+def test_join_on_random_graph_bit_exact(torch_dev, k, mult):
+    """Random neighbour lists (as after an init of tiny leaves): nearly every one of
+    the K*K two-hop candidates is a distinct id, the worst case for the join's
+    per-row tables."""
+    torch, dev = torch_dev
+    import knng
+
+    n, d = 20000, 1024
+    x = synth.mixture(n, d, 200, seed=41)
+    codes_ref, sk_ref = oracle.quantize(x)
+    rng = np.random.default_rng(5)
+    ids_ref = np.empty((n, k), np.int32)
+    for i in range(n):
+        row = rng.choice(n - 1, size=k, replace=False)
+        ids_ref[i] = row + (row >= i)
+    c32 = codes_ref.astype(np.int32)
+    sc_ref = np.einsum("id,ikd->ik", c32, c32[ids_ref]).astype(np.int32)
+    o = np.argsort(-sc_ref, axis=1, kind="stable")
+    ids_ref = np.ascontiguousarray(np.take_along_axis(ids_ref, o, axis=1))
+    sc_ref = np.ascontiguousarray(np.take_along_axis(sc_ref, o, axis=1))
+    prm = _stable(k_build=k, k_eval=min(15, k), rerank_mult=mult)
+    codes = torch.from_numpy(codes_ref).to(dev)
+    sk = torch.from_numpy(sk_ref.view(np.int64)).to(dev)
+    ids = torch.from_numpy(ids_ref.copy()).to(dev)
+    sc = torch.from_numpy(sc_ref.copy()).to(dev)
+    with knng.Context(k_build=k, k_eval=min(15, k), rerank_mult=mult) as ctx:
+        for _ in range(2):
+            up_ref = oracle.join_iter(codes_ref, sk_ref, ids_ref, sc_ref, prm)
+            ids, sc, up = ctx.join_iter(codes, sk, ids, sc)
+            assert up == up_ref
+            np.testing.assert_array_equal(sc.cpu().numpy(), sc_ref)
+            np.testing.assert_array_equal(ids.cpu().numpy(), ids_ref)
