@@ -34,7 +34,7 @@
 //   A  own list, sketch, code row; clear table and histogram; insert the
 //      starting list's ids with a real score, flagged (bit 31 of the key)
 //   B  two-hop ids: warp per neighbour row (K contiguous ids), insert each,
-//      record its slot per j
+//      record its slot per j and the first j per slot (atomicMin)
 //   C  Hamming once per distinct id (the first occurrence of an id appends
 //      its slot to the distinct list during B); CB candidates in flight per
 //      8-lane group (the autotuned candidate block):
@@ -47,7 +47,6 @@
 //      is selected from its h and first j
 //   F  selected ids not flagged as starting-list members: dp4a dots, 8 lanes
 //      per candidate; keep those above the starting pool[K-1].score
-//   F3 first occurrence j of each survivor (one pass, only when there are any)
 //   G  rank-sort the survivors by (h desc, first j asc)
 //   H  sequential insertion + write-back + update count (warp 0)
 // Per row HBM/L2 bytes: K*8 (own list) + K*K*4 (two-hop ids) + d + d/8 (own
@@ -65,15 +64,13 @@ constexpr int kGroups = kThreads / 8;  // 8-lane groups per CTA
 constexpr int kHBins = 1025;
 constexpr int32_t kEmpty = 0x7fffffff;     // never a valid id (num_trees * n < 2^31)
 constexpr uint32_t kPoolFlag = 0x80000000u; // key bit: id is in the starting list with a real score
-constexpr uint32_t kSelFlag = 0x80000000u;  // meta bit 31: selected for rerank
-constexpr uint32_t kPromFlag = 0x40000000u; // meta bit 30: promising; bits 0..12 index it
-constexpr uint32_t kIdxMask = 0x1fffu;
+constexpr uint32_t kFirstMask = 0x1fffu;    // meta bits 0..12: first j (8191 = none)
 
 struct JoinSmem {
   int K, R, KK, d, W, HT;
   size_t bytes;
-  size_t o_code, o_sk, o_slot, o_key, o_meta, o_hist, o_ulist, o_need, o_pkey, o_pid, o_pdot, o_pfirst, o_order,
-      o_pool_id, o_pool_sc;
+  size_t o_code, o_sk, o_slot, o_key, o_meta, o_hist, o_ulist, o_need, o_pkey, o_pid, o_pdot, o_order, o_pool_id,
+      o_pool_sc;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -94,12 +91,11 @@ __host__ __device__ inline JoinSmem join_smem(int K, int R, int d) {
   s.o_key = o;     o = align16(o + size_t(s.HT) * 4);
   s.o_meta = o;    o = align16(o + size_t(s.HT) * 4);
   s.o_hist = o;    o = align16(o + size_t(kHBins) * 4);
-  s.o_ulist = o;   o = align16(o + size_t(s.KK + K) * 2);  // <= K starting-list + K*K candidate slots
+  s.o_ulist = o;   o = align16(o + size_t(s.KK) * 2);
   s.o_need = o;    o = align16(o + size_t(R) * 2);
   s.o_pkey = o;    o = align16(o + size_t(R) * 4);
   s.o_pid = o;     o = align16(o + size_t(R) * 4);
   s.o_pdot = o;    o = align16(o + size_t(R) * 4);
-  s.o_pfirst = o;  o = align16(o + size_t(R) * 4);
   s.o_order = o;   o = align16(o + size_t(R) * 2);
   s.o_pool_id = o; o = align16(o + size_t(K) * 4);
   s.o_pool_sc = o; o = align16(o + size_t(K) * 4);
@@ -124,17 +120,13 @@ __device__ __forceinline__ uint32_t hash_slot(int32_t id, uint32_t mask) {
 
 // Find or insert id (flagged keys match by their low 31 bits).  The table
 // always has free slots (load <= 2/3), so the probe ends; the bound is a guard.
-__device__ __forceinline__ int table_insert(int32_t* key, uint32_t mask, int32_t id, uint32_t flag, bool& created) {
+__device__ __forceinline__ int table_insert(int32_t* key, uint32_t mask, int32_t id, uint32_t flag) {
   uint32_t s = hash_slot(id, mask);
-  created = false;
   for (uint32_t probe = 0; probe <= mask; ++probe) {
     int32_t k = key[s];
     if (k == kEmpty) {
       const int32_t prev = atomicCAS(&key[s], kEmpty, int32_t(uint32_t(id) | flag));
-      if (prev == kEmpty) {
-        created = true;
-        return int(s);
-      }
+      if (prev == kEmpty) return int(s);
       k = prev;
     }
     if ((uint32_t(k) & 0x7fffffffu) == uint32_t(id)) return int(s);
@@ -162,7 +154,6 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   uint32_t* pkey = reinterpret_cast<uint32_t*>(smem + L.o_pkey);
   int32_t* pid = reinterpret_cast<int32_t*>(smem + L.o_pid);
   int32_t* pdot = reinterpret_cast<int32_t*>(smem + L.o_pdot);
-  int32_t* pfirst = reinterpret_cast<int32_t*>(smem + L.o_pfirst);
   uint16_t* order = reinterpret_cast<uint16_t*>(smem + L.o_order);
   int32_t* pool_id = reinterpret_cast<int32_t*>(smem + L.o_pool_id);
   int32_t* pool_sc = reinterpret_cast<int32_t*>(smem + L.o_pool_sc);
@@ -201,7 +192,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;
     for (int t = tid; t < L.HT / 4; t += kThreads) {
       reinterpret_cast<uint4*>(key)[t] = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
-      reinterpret_cast<uint4*>(meta)[t] = make_uint4(0, 0, 0, 0);
+      reinterpret_cast<uint4*>(meta)[t] = make_uint4(kFirstMask, kFirstMask, kFirstMask, kFirstMask);
     }
     if (tid == 0) {
       s_cnt = 0;
@@ -210,17 +201,13 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       s_nprom = 0;
     }
     __syncthreads();
-    for (int k = tid; k < K; k += kThreads) {  // starting-list ids join the distinct list
+    for (int k = tid; k < K; k += kThreads) {
       const int32_t id = pool_id[k];
-      bool created = false;
-      if (pool_sc[k] != kScoreMinI && id >= 0 && id < n) {
-        const int sl = table_insert(key, mask, id, kPoolFlag, created);
-        if (created) ulist[atomicAdd(&s_nu, 1)] = int16_t(sl);
-      }
+      if (pool_sc[k] != kScoreMinI && id >= 0 && id < n) table_insert(key, mask, id, kPoolFlag);
     }
     __syncthreads();
     // ---- B  (warp per neighbour row, all of the warp's rows loaded first; the
-    //         occurrence that creates a slot appends it to the distinct list)
+    //         first occurrence to touch a slot appends it to the distinct list)
     {
       constexpr int kRowsPerWarp = kMaxK / kWarps;  // 8
       int32_t v[2 * kRowsPerWarp];
@@ -242,9 +229,12 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
         bool first = false;
         if (k < K && k2 < K) {
           const int j = k * K + k2;
-          if (n2 >= 0 && n2 < n && n2 != i) sl = table_insert(key, mask, n2, 0u, first);
+          if (n2 >= 0 && n2 < n && n2 != i) sl = table_insert(key, mask, n2, 0u);
           cand_slot[j] = int16_t(sl);
-          if (sl >= 0) ++local_cnt;
+          if (sl >= 0) {
+            first = atomicMin(&meta[sl], uint32_t(j)) == kFirstMask;
+            ++local_cnt;
+          }
         }
         const unsigned bal = __ballot_sync(0xffffffffu, first);
         int base = 0;
@@ -279,7 +269,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
           pc += __shfl_xor_sync(0xffffffffu, pc, 1);
           pc += __shfl_xor_sync(0xffffffffu, pc, 2);
           pc += __shfl_xor_sync(0xffffffffu, pc, 4);
-          if (sub == 0 && sl[u] >= 0) meta[sl[u]] = uint32_t(1024 - pc) << 16;
+          if (sub == 0 && sl[u] >= 0) meta[sl[u]] = (uint32_t(1024 - pc) << 16) | (meta[sl[u]] & kFirstMask);
         }
       }
     }
@@ -332,8 +322,8 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     }
     __syncthreads();
     // ---- E  tie cut: the j of the (R - count(h > h_t))-th occurrence with h == h_t
-    //         (thread-contiguous segments keep the j order); then every selected
-    //         occurrence marks its slot
+    //         (thread-contiguous segments keep the j order); a distinct id with
+    //         h == h_t is selected iff its first occurrence is at or before it
     {
       const int ht = s_ht, need_eq = R - s_gt;
       if (ht >= 0) {
@@ -364,25 +354,17 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
             }
           }
         }
-        __syncthreads();
-        const int jcut = s_jcut;
-        for (int j = j0; j < j1; ++j) {
-          const int sl = cand_slot[j];
-          if (sl < 0) continue;
-          const int h = int((meta[sl] >> 16) & 0x7ffu);
-          if (h > ht || (h == ht && j <= jcut)) atomicOr(&meta[sl], kSelFlag);
-        }
       }
     }
     __syncthreads();
     // ---- F1  selected distinct ids that are not starting-list members need a dot
-    //          (with h_t < 0 every candidate is selected; the distinct list's
-    //          slots without occurrences are starting-list members)
     {
-      const bool all = s_ht < 0;
+      const int ht = s_ht, jcut = ht >= 0 ? s_jcut : 0;
       for (int q = tid; q < nu; q += kThreads) {
         const int sl = ulist[q];
-        const bool sel = all || (meta[sl] & kSelFlag);
+        const uint32_t m = meta[sl];
+        const int h = int((m >> 16) & 0x7ffu);
+        const bool sel = ht < 0 || h > ht || (h == ht && int(m & kFirstMask) <= jcut);
         if (sel && !(uint32_t(key[sl]) & kPoolFlag)) need[atomicAdd(&s_nneed, 1)] = int16_t(sl);
       }
     }
@@ -412,32 +394,15 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
         acc += __shfl_xor_sync(0xffffffffu, acc, 2);
         acc += __shfl_xor_sync(0xffffffffu, acc, 4);
         if (sub == 0 && sl >= 0 && acc > thr0) {
+          const uint32_t m = meta[sl];
           const int slot = atomicAdd(&s_nprom, 1);
-          pkey[slot] = uint32_t(sl);
+          pkey[slot] = (((m >> 16) & 0x7ffu) << 13) | (kFirstMask - (m & kFirstMask));
           pid[slot] = id;
           pdot[slot] = acc;
-          pfirst[slot] = 0x7fffffff;
-          meta[sl] |= kPromFlag | uint32_t(slot);  // one writer per distinct slot
         }
       }
     }
     __syncthreads();
-    // ---- F3  first occurrence (visit-order tie key) of the promising ids only
-    if (s_nprom > 0) {
-      for (int j = tid; j < KK; j += kThreads) {
-        const int sl = cand_slot[j];
-        if (sl >= 0) {
-          const uint32_t m = meta[sl];
-          if (m & kPromFlag) atomicMin(&pfirst[m & kIdxMask], j);
-        }
-      }
-      __syncthreads();
-      for (int p = tid; p < s_nprom; p += kThreads) {
-        const int sl = int(pkey[p]);
-        pkey[p] = (((meta[sl] >> 16) & 0x7ffu) << 13) | uint32_t(kIdxMask - uint32_t(pfirst[p]));
-      }
-      __syncthreads();
-    }
     // ---- G  rank sort by (h desc, first j asc); keys are distinct
     const int P = s_nprom;
     for (int p = tid; p < P; p += kThreads) {
