@@ -275,8 +275,8 @@ def run_batched(args):
                 res, st = ctx.build_batch(xs, st)
                 bt.append(st.device_s)
                 launches += st.kernel_launches
-        for x in xs[:2]:
-            ctx.build(x)  # warm the single-build path
+        for x in xs:
+            ctx.build(x)  # warm the plain path too (autotune buckets, buffers)
         seq = []
         same = True
         for _ in range(max(1, args.steps // 2)):

@@ -135,8 +135,9 @@ int knng_build(knng_ctx* ctx, const void* rows, int64_t n, int d, int rows_on_de
  * merge, one persistent join launch per iteration over every job's rows, the
  * NN-Descent phase replayed as a CUDA graph.  Each job keeps its own pivots,
  * random fills and early stop (src/main.cpp:432-439), so its knns/dists are
- * bit-identical to knng_build of that job alone.  stats (may be NULL) sums
- * the groups. */
+ * bit-identical to knng_build of that job alone.  Groups of different d run
+ * concurrently, each on its own internal context and stream.  stats (may be
+ * NULL): stage times summed over groups, device_s = the batch's span. */
 int knng_build_batch(knng_ctx* ctx, knng_job* jobs, int count, knng_stats* stats);
 
 /* ---- serving loop (no counterpart in the reference) ----

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include <atomic>
+#include <thread>
 #include <cmath>
 #include <map>
 
@@ -68,6 +69,7 @@ struct knng_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   cudaEvent_t jev[2] = {};
+  cudaEvent_t bev = nullptr;  // start of a batch (all dimension groups wait on it)
   cudaEvent_t itev[kMaxIterEvents] = {};
   std::string last_error;
   DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs;
@@ -76,6 +78,7 @@ struct knng_ctx {
   std::vector<uintptr_t> join_graph_key;
   // autotuned join configuration per (d, log2 rows): (ctas_per_sm, cblock)
   std::map<std::pair<int, int>, std::pair<int, int>> tuned;
+  std::vector<knng_ctx*> subs;  // contexts of the second and later dimension groups of a batch
   std::vector<DevBuf*> buffers() {
     return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs};
   }
@@ -547,6 +550,10 @@ int knng_create(knng_ctx** out, const knng_params* p) {
       knng_destroy(c);
       return KNNG_E_CUDA;
     }
+  if ((e = cudaEventCreate(&c->bev))) {
+    knng_destroy(c);
+    return KNNG_E_CUDA;
+  }
   for (DevBuf* b : c->buffers()) b->s = c->stream;
   *out = c;
   return KNNG_OK;
@@ -556,11 +563,13 @@ void knng_destroy(knng_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (knng_ctx* sub : c->subs) knng_destroy(sub);
   if (c->join_graph) cudaGraphExecDestroy(c->join_graph);
   for (DevBuf* b : c->buffers()) b->release();
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& ev : c->itev)
     if (ev) cudaEventDestroy(ev);
+  if (c->bev) cudaEventDestroy(c->bev);
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : c->jev)
@@ -682,6 +691,7 @@ int knng_trim(knng_ctx* c) {
     c->join_graph_key.clear();
   }
   for (DevBuf* b : c->buffers()) b->release();
+  for (knng_ctx* sub : c->subs) knng_trim(sub);
   return KNNG_OK;
 }
 
@@ -696,47 +706,79 @@ int knng_build_batch(knng_ctx* c, knng_job* jobs, int count, knng_stats* stats) 
   knng_stats local{};
   knng_stats& S = stats ? *stats : local;
   std::memset(&S, 0, sizeof(S));
-  // one problem per dimension: jobs of equal d are laid out back to back
+  // one problem per dimension: jobs of equal d are laid out back to back; the
+  // groups run concurrently, each on its own context and stream
   std::vector<int> dims;
   for (int b = 0; b < count; ++b)
     if (std::find(dims.begin(), dims.end(), jobs[b].d) == dims.end()) dims.push_back(jobs[b].d);
-  for (int d : dims) {
-    std::vector<BJob> group;
-    std::vector<int> idx;
-    for (int b = 0; b < count; ++b)
-      if (jobs[b].d == d) {
-        group.push_back(BJob{jobs[b].rows, jobs[b].n, jobs[b].rows_on_device, jobs[b].knns, jobs[b].dists,
-                             jobs[b].out_on_device, 0});
-        idx.push_back(b);
-      }
-    knng_stats gs{};
-    int st = run_batch(c, group.data(), int(group.size()), d, gs);
-    for (size_t g = 0; g < group.size(); ++g) {
-      jobs[idx[g]].status = st;
-      jobs[idx[g]].iterations = group[g].iterations;
-    }
-    if (st) return st;
-    S.quantize_s += gs.quantize_s;
-    S.forest_s += gs.forest_s;
-    S.init_s += gs.init_s;
-    S.join_s += gs.join_s;
-    S.export_s += gs.export_s;
-    S.build_s += gs.build_s;
-    S.device_s += gs.device_s;
-    S.kernel_launches += gs.kernel_launches;
-    S.forest_levels = std::max(S.forest_levels, gs.forest_levels);
-    S.leaves += gs.leaves;
-    S.iterations = std::max(S.iterations, gs.iterations);
-    for (int it = 0; it < 64; ++it) {
-      S.updates[it] += gs.updates[it];
-      S.join_ms[it] += gs.join_ms[it];
-      S.join_candidates[it] += gs.join_candidates[it];
-      S.join_dots[it] += gs.join_dots[it];
-    }
-    S.join_ctas_per_sm = gs.join_ctas_per_sm;
-    S.join_cblock = gs.join_cblock;
-    S.graph_used = gs.graph_used;
+  const int G = int(dims.size());
+  while (int(c->subs.size()) < G - 1) {
+    knng_ctx* sub = nullptr;
+    const int st = knng_create(&sub, &c->prm);
+    if (st) return set_error(c, st, "context for a dimension group");
+    c->subs.push_back(sub);
   }
+  std::vector<std::vector<BJob>> groups(G);
+  std::vector<std::vector<int>> idx(G);
+  for (int g = 0; g < G; ++g)
+    for (int b = 0; b < count; ++b)
+      if (jobs[b].d == dims[g]) {
+        groups[g].push_back(BJob{jobs[b].rows, jobs[b].n, jobs[b].rows_on_device, jobs[b].knns, jobs[b].dists,
+                                 jobs[b].out_on_device, 0});
+        idx[g].push_back(b);
+      }
+  std::vector<knng_stats> gs(G);
+  std::vector<int> gst(G, KNNG_OK);
+  cudaEventRecord(c->bev, c->stream);  // batch start: every group's stream waits for it
+  auto run_group = [&](int g) {
+    knng_ctx* gc = g == 0 ? c : c->subs[size_t(g - 1)];
+    cudaSetDevice(gc->device);
+    cudaStreamWaitEvent(gc->stream, c->bev, 0);
+    gst[g] = run_batch(gc, groups[g].data(), int(groups[g].size()), dims[g], gs[g]);
+    if (gst[g] && gc != c) c->last_error = gc->last_error;
+  };
+  if (G == 1) {
+    run_group(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int g = 1; g < G; ++g) th.emplace_back(run_group, g);
+    run_group(0);
+    for (auto& t : th) t.join();
+  }
+  float span_ms = 0.f;
+  for (int g = 0; g < G; ++g) {
+    knng_ctx* gc = g == 0 ? c : c->subs[size_t(g - 1)];
+    for (size_t q = 0; q < groups[g].size(); ++q) {
+      jobs[idx[g][q]].status = gst[g];
+      jobs[idx[g][q]].iterations = groups[g][q].iterations;
+    }
+    if (gst[g] == KNNG_OK) span_ms = std::max(span_ms, elapsed(c->bev, gc->ev[5]));
+  }
+  for (int g = 0; g < G; ++g)
+    if (gst[g]) return gst[g];
+  for (int g = 0; g < G; ++g) {
+    S.quantize_s += gs[g].quantize_s;
+    S.forest_s += gs[g].forest_s;
+    S.init_s += gs[g].init_s;
+    S.join_s += gs[g].join_s;
+    S.export_s += gs[g].export_s;
+    S.build_s += gs[g].build_s;
+    S.kernel_launches += gs[g].kernel_launches;
+    S.forest_levels = std::max(S.forest_levels, gs[g].forest_levels);
+    S.leaves += gs[g].leaves;
+    S.iterations = std::max(S.iterations, gs[g].iterations);
+    for (int it = 0; it < 64; ++it) {
+      S.updates[it] += gs[g].updates[it];
+      S.join_ms[it] += gs[g].join_ms[it];
+      S.join_candidates[it] += gs[g].join_candidates[it];
+      S.join_dots[it] += gs[g].join_dots[it];
+    }
+    S.join_ctas_per_sm = gs[g].join_ctas_per_sm;
+    S.join_cblock = gs[g].join_cblock;
+    S.graph_used = gs[g].graph_used;
+  }
+  // stage sums add up the groups' own times; device_s is the batch's span
+  S.device_s = span_ms * 1e-3;
   return KNNG_OK;
 }
 
