@@ -45,6 +45,7 @@ enum { KNNG_QUANT_TRUNC = 0, KNNG_QUANT_ROUND = 1 };
 enum { KNNG_JOIN_JACOBI = 0, KNNG_JOIN_INPLACE = 1 };
 enum { KNNG_ORDER_NATURAL = 0, KNNG_ORDER_LEAF = 1 };
 enum { KNNG_GRAM_DP4A = 0, KNNG_GRAM_TCGEN05 = 1 };
+enum { KNNG_INIT_FOREST = 0, KNNG_INIT_RANDOM = 1 };
 
 /* Build parameters.  Defaults (knng_default_params) are the reference's
  * compile-time constants, src/main.cpp:19-29. */
@@ -65,6 +66,8 @@ typedef struct knng_params {
   int autotune;          /* 1: time the join configurations once per (d, size) */
   int use_graph;         /* 1: replay the NN-Descent phase as a CUDA graph */
   int gram_mode;         /* leaf Gram: KNNG_GRAM_DP4A or KNNG_GRAM_TCGEN05 (bf16 tensor cores) */
+  int init_mode;         /* KNNG_INIT_FOREST (src/main.cpp) or KNNG_INIT_RANDOM, the archived
+                            variant archive/nndescent_optimized.cpp:97-118 (needs n > k_build) */
 } knng_params;
 
 /* Per-build timings and convergence record (seconds, device-timed). */

@@ -323,6 +323,42 @@ int oracle_init(const int8_t* codes, int64_t n, int d, const oracle_params* prm,
 }
 
 // ---------------------------------------------------------------------------
+// Random initial graph, the archived variant archive/nndescent_optimized.cpp:
+// 97-118 (K random neighbours per row scored by exact int8 dot, sorted by score
+// descending).  The archive draws from one std::mt19937 per OpenMP thread, so
+// its graph depends on the thread count; here row i draws from xorshift32 with
+// state seed + i (the reference's fill stream, src/main.cpp:271-276), skipping
+// i and ids already drawn, and ties are ordered by id ascending.
+int oracle_init_random(const int8_t* codes, int64_t n, int d, const oracle_params* prm, int32_t* ids,
+                       int32_t* scores) {
+  const int K = prm->k_build;
+  if (n <= K) return -1;
+  set_threads(prm->threads);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    std::vector<Neighbor> pool;
+    uint32_t rs = prm->seed + uint32_t(i);
+    while (int(pool.size()) < K) {
+      rs = xorshift32(rs);
+      const int64_t r = int64_t(uint64_t(rs) % uint64_t(n));
+      if (r == i) continue;
+      bool dup = false;
+      for (const Neighbor& q : pool) dup |= q.id == r;
+      if (dup) continue;
+      pool.push_back({int(r), dot_i8(codes + i * d, codes + r * d, d)});
+    }
+    std::sort(pool.begin(), pool.end(), [](const Neighbor& a, const Neighbor& b) {
+      return a.score != b.score ? a.score > b.score : a.id < b.id;
+    });
+    for (int k = 0; k < K; ++k) {
+      ids[i * K + k] = pool[k].id;
+      scores[i * K + k] = pool[k].score;
+    }
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
 // a5: one NN-Descent iteration.  src/main.cpp:324-430.
 // Row i: candidates are G[G[i][k]][k2] for k, k2 < K in that order, minus i,
 // each scored h = 1024 - sum_w popcount(b_i[w] ^ b_c[w]); the best R = K *

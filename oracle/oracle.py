@@ -66,6 +66,7 @@ def lib():
                                     C.c_void_p, C.c_int64, P(C.c_int64)]
         L.oracle_init.argtypes = [C.c_void_p, C.c_int64, C.c_int, P(Params), C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p]
+        L.oracle_init_random.argtypes = [C.c_void_p, C.c_int64, C.c_int, P(Params), C.c_void_p, C.c_void_p]
         L.oracle_join_iter.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int64, C.c_int, P(Params),
                                        C.c_void_p, C.c_void_p]
         L.oracle_join_iter.restype = C.c_int64
@@ -132,6 +133,17 @@ def init_graph(codes, perm, leaf_flag, prm=None):
                            _ptr(ids), _ptr(sc))
     if rc:
         raise ValueError("oracle_init failed")
+    return ids, sc
+
+
+def init_random(codes, prm=None):
+    """Random initial graph (archive/nndescent_optimized.cpp:97-118, xorshift32 per row)."""
+    prm = prm or params()
+    n, d = codes.shape
+    ids = np.empty((n, prm.k_build), np.int32)
+    sc = np.empty((n, prm.k_build), np.int32)
+    if lib().oracle_init_random(_ptr(np.ascontiguousarray(codes)), n, d, C.byref(prm), _ptr(ids), _ptr(sc)):
+        raise ValueError("oracle_init_random failed")
     return ids, sc
 
 

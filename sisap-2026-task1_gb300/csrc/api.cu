@@ -113,6 +113,7 @@ int check_params(knng_ctx* c, const knng_params& p) {
   if (p.join_mode != KNNG_JOIN_JACOBI && p.join_mode != KNNG_JOIN_INPLACE) return set_error(c, KNNG_E_ARGS, "bad join_mode");
   if (p.row_order != KNNG_ORDER_NATURAL && p.row_order != KNNG_ORDER_LEAF) return set_error(c, KNNG_E_ARGS, "bad row_order");
   if (p.gram_mode != KNNG_GRAM_DP4A && p.gram_mode != KNNG_GRAM_TCGEN05) return set_error(c, KNNG_E_ARGS, "bad gram_mode");
+  if (p.init_mode != KNNG_INIT_FOREST && p.init_mode != KNNG_INIT_RANDOM) return set_error(c, KNNG_E_ARGS, "bad init_mode");
   return KNNG_OK;
 }
 
@@ -361,14 +362,25 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     if ((st = quantize_input(c, jobs[b].rows, jobs[b].n, d, jobs[b].on_dev, hoff[b]))) return st;
   cudaEventRecord(c->ev[1], str);
   int64_t levels = 0, leaves = 0;
-  if ((st = run_forest(c->codes.as<int8_t>(), N, d, T, p.leaf_size, p.seed, nullptr, 0, c->perm.as<int32_t>(),
-                       c->leaf_flag.as<uint8_t>(), s.fb, str, &levels, &c->last_error, jt, split)))
+  const bool random_init = p.init_mode == KNNG_INIT_RANDOM;
+  if (random_init) {
+    for (int b = 0; b < J; ++b)
+      if (hn[b] <= K) return set_error(c, KNNG_E_ARGS, "random init needs n > k_build for every job");
+  } else if ((st = run_forest(c->codes.as<int8_t>(), N, d, T, p.leaf_size, p.seed, nullptr, 0, c->perm.as<int32_t>(),
+                              c->leaf_flag.as<uint8_t>(), s.fb, str, &levels, &c->last_error, jt, split))) {
     return st;
+  }
   cudaEventRecord(c->ev[2], str);
-  if ((st = run_init(c->codes.as<int8_t>(), N, d, T, p.leaf_size, K, p.seed, c->perm.as<int32_t>(),
-                     c->leaf_flag.as<uint8_t>(), ids[0], scs[0], s.ib, str, &leaves, &c->last_error, jt, p.gram_mode)))
+  if (random_init) {
+    if ((e = launch_init_random(c->codes.as<int8_t>(), d, N, K, p.seed, jt, ids[0], scs[0], c->num_sms, str)))
+      return cuda_fail(c, e, "random init");
+  } else if ((st = run_init(c->codes.as<int8_t>(), N, d, T, p.leaf_size, K, p.seed, c->perm.as<int32_t>(),
+                            c->leaf_flag.as<uint8_t>(), ids[0], scs[0], s.ib, str, &leaves, &c->last_error, jt,
+                            p.gram_mode))) {
     return st;
-  const int32_t* order = p.row_order == KNNG_ORDER_LEAF ? c->perm.as<int32_t>() : nullptr;
+  }
+  // rows in tree-0 leaf order (no forest with the random init: natural order)
+  const int32_t* order = (p.row_order == KNNG_ORDER_LEAF && !random_init) ? c->perm.as<int32_t>() : nullptr;
   const std::pair<int, int> cfg = autotune_join(c, N, d, ids, scs, order, tune_counters);
   cudaEventRecord(c->ev[3], str);
   // NN-Descent, captured once per launch key and replayed
@@ -377,7 +389,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->sketch.p), uintptr_t(c->graph.p),
                                         uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(N), uintptr_t(d),
                                         uintptr_t(J), uintptr_t(o), uintptr_t(cfg.first), uintptr_t(cfg.second),
-                                        uintptr_t(p.row_order), uintptr_t(p.join_mode), uintptr_t(MI),
+                                        uintptr_t(order != nullptr), uintptr_t(p.join_mode), uintptr_t(MI),
                                         uintptr_t(K), uintptr_t(p.rerank_mult)};
     if (!c->join_graph || c->join_graph_key != key) {
       if (c->join_graph) {
@@ -495,6 +507,7 @@ void knng_default_params(knng_params* p) {
   p->autotune = 1;
   p->use_graph = 1;
   p->gram_mode = KNNG_GRAM_TCGEN05;
+  p->init_mode = KNNG_INIT_FOREST;
 }
 
 const char* knng_status_string(int s) {

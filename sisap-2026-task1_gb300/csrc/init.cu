@@ -286,6 +286,71 @@ __global__ void init_fixup(const int8_t* __restrict__ codes, int d, int64_t n_to
   }
 }
 
+// Random initial graph (archived variant archive/nndescent_optimized.cpp:97-118):
+// row i draws K distinct ids from xorshift32 with state seed + (job-local) i,
+// skipping itself, scores them by exact int8 dot and keeps them ordered by
+// (score desc, id asc).  One warp per row: lane 0 draws, every lane scores
+// candidates lane and lane + 32, the warp inserts them into its sorted list.
+__global__ void __launch_bounds__(256) init_random_kernel(const int8_t* __restrict__ codes, int d, int64_t n_total,
+                                                          int K, uint32_t seed, JobTable jt,
+                                                          int32_t* __restrict__ ids, int32_t* __restrict__ scores) {
+  __shared__ int32_t drawn[8][kMaxK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t warps = int64_t(gridDim.x) * 8;
+  for (int64_t gi = int64_t(blockIdx.x) * 8 + w; gi < n_total; gi += warps) {
+    const int b = job_of(jt, gi);
+    const int64_t base = jt.off[b], n = jt.n[b], i = gi - base;
+    if (lane == 0) {
+      uint32_t rs = seed + uint32_t(i);
+      int c = 0;
+      for (int budget = 1 << 22; c < K && budget > 0; --budget) {
+        rs = xorshift32(rs);
+        const int64_t r = int64_t(uint64_t(rs) % uint64_t(n));
+        if (r == i) continue;
+        bool dup = false;
+        for (int q = 0; q < c; ++q) dup |= drawn[w][q] == int32_t(base + r);
+        if (!dup) drawn[w][c++] = int32_t(base + r);
+      }
+      for (; c < K; ++c) drawn[w][c] = int32_t(base + (i + 1 + c) % n);  // budget guard only
+    }
+    __syncwarp();
+    const int4* qi = reinterpret_cast<const int4*>(codes + gi * d);
+    uint64_t key[2] = {0, 0};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int c = lane + 32 * h;
+      if (c < K) {
+        const int4* qc = reinterpret_cast<const int4*>(codes + int64_t(drawn[w][c]) * d);
+        int acc = 0;
+        for (int u = 0; u < d / 16; ++u) {
+          const int4 a = __ldg(qi + u), v = __ldg(qc + u);
+          acc = __dp4a(a.x, v.x, acc);
+          acc = __dp4a(a.y, v.y, acc);
+          acc = __dp4a(a.z, v.z, acc);
+          acc = __dp4a(a.w, v.w, acc);
+        }
+        key[h] = make_key(acc, drawn[w][c]);
+      }
+    }
+    uint64_t kA = 0, kB = 0;
+    for (int h = 0; h < 2; ++h)
+      for (int src = 0; src < 32; ++src) {
+        if (src + 32 * h >= K) break;
+        const uint64_t ck = __shfl_sync(0xffffffffu, key[h], src);
+        list_insert(kA, kB, ck, K, lane);
+      }
+    if (lane < K) {
+      ids[gi * K + lane] = key_id(kA);
+      scores[gi * K + lane] = key_score(kA);
+    }
+    if (32 + lane < K) {
+      ids[gi * K + 32 + lane] = key_id(kB);
+      scores[gi * K + 32 + lane] = key_score(kB);
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void export_kernel(const int32_t* __restrict__ ids, const int32_t* __restrict__ scores, int64_t n,
                               int K, int k_eval, const int32_t* __restrict__ id_map, int32_t* __restrict__ knns,
                               float* __restrict__ dists, JobTable jt) {
@@ -376,6 +441,14 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
     if ((e = cudaGetLastError())) return fail(e, "init fixup");
   }
   return 0;
+}
+
+cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int K, uint32_t seed, const JobTable& jt,
+                               int32_t* ids, int32_t* scores, int num_sms, cudaStream_t s) {
+  const int64_t blocks = std::min<int64_t>((n_total + 7) / 8, int64_t(num_sms) * 16);
+  init_random_kernel<<<unsigned(blocks), 256, 0, s>>>(codes, d, n_total, K, seed, jt, ids, scores);
+  note_launch();
+  return cudaGetLastError();
 }
 
 cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, int K, int k_eval,

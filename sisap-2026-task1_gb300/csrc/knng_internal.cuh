@@ -101,6 +101,10 @@ cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm,
                                 int64_t nleaves, int64_t total, int32_t* gram, unsigned* err, int num_sms,
                                 cudaStream_t s);
 
+// Random initial graph (init_mode KNNG_INIT_RANDOM); every job needs n > K.
+cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int K, uint32_t seed, const JobTable& jt,
+                               int32_t* ids, int32_t* scores, int num_sms, cudaStream_t s);
+
 // ---- join.cu ----
 // Per-batch NN-Descent control block in device memory.
 struct JoinCtl {

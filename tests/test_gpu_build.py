@@ -169,3 +169,36 @@ def test_build_degenerate_duplicates(knng_mod):
     with knng.Context() as ctx:
         knns, dists, st = ctx.build(np.ascontiguousarray(x))
     _check_export(x, knns, dists)
+
+
+def _oracle_random_build(x, max_iter=30):
+    """Random init (archive/nndescent_optimized.cpp) + the reference's iteration and
+    early stop, in the oracle's double-buffered stable-tie mode."""
+    prm = oracle.params(threads=1, tie_mode=oracle.TIE_STABLE, jacobi=1)
+    codes, sk = oracle.quantize(x)
+    ids, sc = oracle.init_random(codes, prm)
+    n, K = ids.shape
+    prev, it = np.float32(1.0), 0
+    for it in range(max_iter):
+        up = oracle.join_iter(codes, sk, ids, sc, prm)
+        rate = np.float32(up) / np.float32(n * K)
+        if rate < np.float32(0.04) or (it > 0 and (prev - rate) < np.float32(0.01)):
+            it += 1
+            break
+        prev = rate
+    else:
+        it = max_iter
+    k, d = oracle.export(ids, sc)
+    return k, d, it
+
+
+@pytest.mark.parametrize("iters", [0, 30])
+def test_random_init_matches_oracle(knng_mod, iters):
+    knng = knng_mod
+    x = synth.mixture(4000, 768, 40, seed=61)
+    with knng.Context(init_mode=knng.INIT_RANDOM, max_iterations=iters) as ctx:
+        k, dd, st = ctx.build(x)
+    kr, dr, itr = _oracle_random_build(x, iters)
+    assert st.iterations == itr
+    np.testing.assert_array_equal(k, kr)
+    np.testing.assert_array_equal(dd, dr)
