@@ -45,4 +45,4 @@ def test_cli_and_evaluator_end_to_end(tmp_path):
     out = subprocess.run(ev + ["gt.h5", "results/task1/apex_simd.h5"], cwd=tmp_path, check=True,
                          capture_output=True, text=True).stdout
     rec = float(out.split("True Recall:")[1].split("%")[0]) / 100
-    assert abs(rec - synth.recall_at_k(ds["knns"], synth.exact_knn(x, 15))) < 1e-9
+    assert abs(rec - synth.recall_at_k(ds["knns"], synth.exact_knn(x, 15))) < 1e-6  # printed to 4 decimals in %
