@@ -18,6 +18,7 @@
 #include <vector>
 
 #include <atomic>
+#include <mutex>
 #include <thread>
 #include <cmath>
 #include <map>
@@ -27,6 +28,7 @@ size_t join_smem_bytes(int K, int R, int d);
 namespace {
 std::atomic<int64_t> g_launches{0};
 }
+std::mutex g_capture_mu;
 int64_t launches() { return g_launches.load(std::memory_order_relaxed); }
 void note_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 }  // namespace knng
@@ -272,7 +274,7 @@ std::pair<int, int> autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const 
 // the per-job stop check; launches after every job has stopped do nothing.
 cudaError_t join_phase(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int32_t* const scs[2],
                        const int32_t* order, const JobTable& jt, const JoinCtl& ctl, unsigned long long* counters,
-                       std::pair<int, int> cfg, bool capture) {
+                       std::pair<int, int> cfg, bool capture, const char** step) {
   const knng_params& p = c->prm;
   const int K = p.k_build;
   const bool jac = p.join_mode == KNNG_JOIN_JACOBI;
@@ -282,15 +284,16 @@ cudaError_t join_phase(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int
     const int nxt = jac ? 1 - cur : cur;
     e = capture ? cudaEventRecordWithFlags(c->itev[2 * it], c->stream, cudaEventRecordExternal)
                 : cudaEventRecord(c->itev[2 * it], c->stream);
-    if (e) return e;
+    if (e) return (*step = "iteration start event", e);
     if ((e = launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[cur],
                          scs[cur], ids[nxt], scs[nxt], order, counters + 3 * it, c->num_sms, c->stream, &jt, &ctl,
                          cfg.first, cfg.second)))
-      return e;
+      return (*step = "join launch", e);
     e = capture ? cudaEventRecordWithFlags(c->itev[2 * it + 1], c->stream, cudaEventRecordExternal)
                 : cudaEventRecord(c->itev[2 * it + 1], c->stream);
-    if (e) return e;
-    if ((e = launch_stop_check(jt, ctl, K, it, nxt, p.early_stop_rate, p.rate_diff_tol, c->stream))) return e;
+    if (e) return (*step = "iteration end event", e);
+    if ((e = launch_stop_check(jt, ctl, K, it, nxt, p.early_stop_rate, p.rate_diff_tol, c->stream)))
+      return (*step = "stop check", e);
     cur = nxt;
   }
   return cudaSuccess;
@@ -385,6 +388,8 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   cudaEventRecord(c->ev[3], str);
   // NN-Descent, captured once per launch key and replayed
   bool graph_used = false;
+  if ((e = join_prepare(K, K * p.rerank_mult, d, cfg.first, cfg.second))) return cuda_fail(c, e, "join variant");
+  const char* step = "";
   if (p.use_graph) {
     const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->sketch.p), uintptr_t(c->graph.p),
                                         uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(N), uintptr_t(d),
@@ -397,8 +402,9 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
         c->join_graph = nullptr;
       }
       cudaGraph_t g = nullptr;
+      std::lock_guard<std::mutex> capture_lock(g_capture_mu);  // one capture at a time per process
       if (cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        const cudaError_t ce = join_phase(c, N, d, ids, scs, order, jt, ctl, ctl.counters, cfg, true);
+        const cudaError_t ce = join_phase(c, N, d, ids, scs, order, jt, ctl, ctl.counters, cfg, true, &step);
         const cudaError_t ee = cudaStreamEndCapture(str, &g);
         if (ce == cudaSuccess && ee == cudaSuccess && g &&
             cudaGraphInstantiate(&c->join_graph, g, 0) == cudaSuccess)
@@ -414,8 +420,8 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
       graph_used = true;
     }
   }
-  if (!graph_used && (e = join_phase(c, N, d, ids, scs, order, jt, ctl, ctl.counters, cfg, false)))
-    return cuda_fail(c, e, "join phase");
+  if (!graph_used && (e = join_phase(c, N, d, ids, scs, order, jt, ctl, ctl.counters, cfg, false, &step)))
+    return cuda_fail(c, e, (std::string("join phase (") + step + ")").c_str());
   cudaEventRecord(c->ev[4], str);
   // results of the control block
   std::vector<int> iters(jb);

@@ -54,6 +54,9 @@
 #include "knng_internal.cuh"
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 namespace knng {
 namespace {
@@ -514,18 +517,53 @@ __global__ void stop_check_kernel(JobTable jt, JoinCtl ctl, int K, int iter, int
 
 size_t join_smem_bytes(int K, int R, int d) { return join_smem(K, R, d).bytes; }
 
+// Resident CTAs per SM of a join variant at `smem` bytes of dynamic shared
+// memory.  The attribute is set and the occupancy queried once per process and
+// variant (under a mutex, so concurrent contexts and stream captures never
+// issue these calls); a failure is returned as a CUDA error, not masked.
+std::mutex g_variant_mu;
+std::map<std::tuple<int, int, size_t>, int> g_variant_ctas;
+
 template <int CB, int MINB>
-int max_ctas(size_t smem) {
-  if (cudaFuncSetAttribute(join_kernel<CB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) !=
-      cudaSuccess)
-    return 1;
+cudaError_t max_ctas(size_t smem, int* per_sm_out) {
+  std::lock_guard<std::mutex> lk(g_variant_mu);
+  const auto key = std::make_tuple(CB, MINB, smem);
+  auto it = g_variant_ctas.find(key);
+  if (it != g_variant_ctas.end()) {
+    *per_sm_out = it->second;
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaFuncSetAttribute(join_kernel<CB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, join_kernel<CB, MINB>, kThreads, smem) != cudaSuccess)
-    return 1;
-  return per_sm < 1 ? 1 : per_sm;
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, join_kernel<CB, MINB>, kThreads, smem);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // reported through the return value
+    return e;
+  }
+  per_sm = per_sm < 1 ? 1 : per_sm;
+  g_variant_ctas.emplace(key, per_sm);
+  *per_sm_out = per_sm;
+  return cudaSuccess;
 }
 
-int join_max_ctas_per_sm(int K, int R, int d) { return max_ctas<4, 4>(join_smem(K, R, d).bytes); }
+int join_max_ctas_per_sm(int K, int R, int d) {
+  int per_sm = 1;
+  return max_ctas<4, 4>(join_smem(K, R, d).bytes, &per_sm) == cudaSuccess ? per_sm : 1;
+}
+
+cudaError_t join_prepare(int K, int R, int d, int ctas_per_sm, int cblock) {
+  const size_t smem = join_smem(K, R, d).bytes;
+  int per_sm = 0;
+  if (ctas_per_sm == 3) {
+    if (cblock == 2) return max_ctas<2, 3>(smem, &per_sm);
+    if (cblock == 8) return max_ctas<8, 3>(smem, &per_sm);
+    return max_ctas<4, 3>(smem, &per_sm);
+  }
+  if (cblock == 2) return max_ctas<2, 4>(smem, &per_sm);
+  if (cblock == 8) return max_ctas<8, 4>(smem, &per_sm);
+  return max_ctas<4, 4>(smem, &per_sm);
+}
 
 cudaError_t launch_stop_check(const JobTable& jt, const JoinCtl& ctl, int K, int iter, int out_buf, float stop_rate,
                               float diff_tol, cudaStream_t s) {
@@ -541,24 +579,31 @@ cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, 
   const size_t smem = join_smem(K, R, d).bytes;
   const JobTable no_jobs{};
   const JoinCtl no_ctl{};
-  auto go = [&](auto kern, int max_per_sm) {
+  cudaError_t e = cudaSuccess;
+  auto go = [&](auto kern, cudaError_t qe, int max_per_sm) {
+    if (qe != cudaSuccess) {
+      e = qe;
+      return;
+    }
     const int64_t blocks = std::min<int64_t>(n, int64_t(num_sms) * max_per_sm);
     kern<<<unsigned(blocks), kThreads, smem, s>>>(codes, sketch, n, d, K, R, ids_in, scores_in, ids_out, scores_out,
                                                   row_order, counters, jt ? *jt : no_jobs, ctl ? *ctl : no_ctl);
+    e = cudaGetLastError();
   };
   // ctas_per_sm 3: up to 85 registers per thread (no spills), 3 resident CTAs;
   // otherwise 64 registers, 4 resident CTAs
+  int per_sm = 1;
   if (ctas_per_sm == 3) {
-    if (cblock == 2) go(join_kernel<2, 3>, max_ctas<2, 3>(smem));
-    else if (cblock == 8) go(join_kernel<8, 3>, max_ctas<8, 3>(smem));
-    else go(join_kernel<4, 3>, max_ctas<4, 3>(smem));
+    if (cblock == 2) { cudaError_t q = max_ctas<2, 3>(smem, &per_sm); go(join_kernel<2, 3>, q, per_sm); }
+    else if (cblock == 8) { cudaError_t q = max_ctas<8, 3>(smem, &per_sm); go(join_kernel<8, 3>, q, per_sm); }
+    else { cudaError_t q = max_ctas<4, 3>(smem, &per_sm); go(join_kernel<4, 3>, q, per_sm); }
   } else {
-    if (cblock == 2) go(join_kernel<2, 4>, max_ctas<2, 4>(smem));
-    else if (cblock == 8) go(join_kernel<8, 4>, max_ctas<8, 4>(smem));
-    else go(join_kernel<4, 4>, max_ctas<4, 4>(smem));
+    if (cblock == 2) { cudaError_t q = max_ctas<2, 4>(smem, &per_sm); go(join_kernel<2, 4>, q, per_sm); }
+    else if (cblock == 8) { cudaError_t q = max_ctas<8, 4>(smem, &per_sm); go(join_kernel<8, 4>, q, per_sm); }
+    else { cudaError_t q = max_ctas<4, 4>(smem, &per_sm); go(join_kernel<4, 4>, q, per_sm); }
   }
   note_launch();
-  return cudaGetLastError();
+  return e;
 }
 
 }  // namespace knng

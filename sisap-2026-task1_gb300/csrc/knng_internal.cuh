@@ -132,6 +132,8 @@ cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, 
 cudaError_t launch_stop_check(const JobTable& jt, const JoinCtl& ctl, int K, int iter, int out_buf,
                               float stop_rate, float diff_tol, cudaStream_t s);
 int join_max_ctas_per_sm(int K, int R, int d);
+// Resolve a join variant's launch attributes before any stream capture.
+cudaError_t join_prepare(int K, int R, int d, int ctas_per_sm, int cblock);
 
 // ---- export (init.cu) ----
 cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, int K, int k_eval,
