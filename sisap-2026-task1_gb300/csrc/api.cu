@@ -249,6 +249,10 @@ std::pair<int, int> autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const 
   if (it != c->tuned.end()) return it->second;
   std::pair<int, int> best{4, 4};
   if (!p.autotune || p.join_mode != KNNG_JOIN_JACOBI) return best;
+  if (join_prepare_all(p.k_build, p.k_build * p.rerank_mult, d) != cudaSuccess) {
+    c->last_error = std::string("join variants: ") + join_variant_error();
+    return best;
+  }
   const std::pair<int, int> cand[] = {{4, 4}, {4, 8}, {3, 4}, {3, 8}, {4, 2}};
   float best_ms = 1e30f;
   const int K = p.k_build;
@@ -388,7 +392,8 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   cudaEventRecord(c->ev[3], str);
   // NN-Descent, captured once per launch key and replayed
   bool graph_used = false;
-  if ((e = join_prepare(K, K * p.rerank_mult, d, cfg.first, cfg.second))) return cuda_fail(c, e, "join variant");
+  if ((e = join_prepare(K, K * p.rerank_mult, d, cfg.first, cfg.second)))
+    return cuda_fail(c, e, (std::string("join variant: ") + join_variant_error()).c_str());
   const char* step = "";
   if (p.use_graph) {
     const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->sketch.p), uintptr_t(c->graph.p),
@@ -574,6 +579,12 @@ int knng_create(knng_ctx** out, const knng_params* p) {
     return KNNG_E_CUDA;
   }
   for (DevBuf* b : c->buffers()) b->s = c->stream;
+  // resolve the join kernels' launch attributes now, outside any capture
+  for (int d : {128, 256, 384, 512, 640, 768, 896, 1024})
+    if ((e = join_prepare_all(c->prm.k_build, c->prm.k_build * c->prm.rerank_mult, d))) {
+      c->last_error = std::string("join variants: ") + join_variant_error();
+      break;
+    }
   *out = c;
   return KNNG_OK;
 }

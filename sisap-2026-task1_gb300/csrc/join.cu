@@ -56,6 +56,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <cstdio>
 #include <tuple>
 
 namespace knng {
@@ -523,6 +524,7 @@ size_t join_smem_bytes(int K, int R, int d) { return join_smem(K, R, d).bytes; }
 // issue these calls); a failure is returned as a CUDA error, not masked.
 std::mutex g_variant_mu;
 std::map<std::tuple<int, int, size_t>, int> g_variant_ctas;
+char g_variant_err[256] = "";
 
 template <int CB, int MINB>
 cudaError_t max_ctas(size_t smem, int* per_sm_out) {
@@ -533,12 +535,22 @@ cudaError_t max_ctas(size_t smem, int* per_sm_out) {
     *per_sm_out = it->second;
     return cudaSuccess;
   }
-  cudaError_t e = cudaFuncSetAttribute(join_kernel<CB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaFuncAttributes fa{};
+  cudaError_t e = cudaFuncGetAttributes(&fa, join_kernel<CB, MINB>);  // loads the function
+  const char* what = "cudaFuncGetAttributes";
+  if (e == cudaSuccess) {
+    e = cudaFuncSetAttribute(join_kernel<CB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    what = "cudaFuncSetAttribute";
+  }
   int per_sm = 0;
-  if (e == cudaSuccess)
+  if (e == cudaSuccess) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, join_kernel<CB, MINB>, kThreads, smem);
+    what = "cudaOccupancyMaxActiveBlocksPerMultiprocessor";
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();  // reported through the return value
+    std::snprintf(g_variant_err, sizeof(g_variant_err), "%s(join_kernel<%d,%d>, smem %zu, static smem %zu, regs %d): %s",
+                  what, CB, MINB, smem, size_t(fa.sharedSizeBytes), fa.numRegs, cudaGetErrorString(e));
     return e;
   }
   per_sm = per_sm < 1 ? 1 : per_sm;
@@ -550,6 +562,17 @@ cudaError_t max_ctas(size_t smem, int* per_sm_out) {
 int join_max_ctas_per_sm(int K, int R, int d) {
   int per_sm = 1;
   return max_ctas<4, 4>(join_smem(K, R, d).bytes, &per_sm) == cudaSuccess ? per_sm : 1;
+}
+
+const char* join_variant_error() { return g_variant_err; }
+
+cudaError_t join_prepare_all(int K, int R, int d) {
+  for (int c : {3, 4})
+    for (int b : {2, 4, 8}) {
+      const cudaError_t e = join_prepare(K, R, d, c, b);
+      if (e != cudaSuccess) return e;
+    }
+  return cudaSuccess;
 }
 
 cudaError_t join_prepare(int K, int R, int d, int ctas_per_sm, int cblock) {

@@ -134,6 +134,8 @@ cudaError_t launch_stop_check(const JobTable& jt, const JoinCtl& ctl, int K, int
 int join_max_ctas_per_sm(int K, int R, int d);
 // Resolve a join variant's launch attributes before any stream capture.
 cudaError_t join_prepare(int K, int R, int d, int ctas_per_sm, int cblock);
+cudaError_t join_prepare_all(int K, int R, int d);  // every variant the autotuner may pick
+const char* join_variant_error();                    // detail of the last failed resolution
 
 // ---- export (init.cu) ----
 cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, int K, int k_eval,
