@@ -356,9 +356,11 @@ int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t 
   if (e) return fail(e, "leaf_flag clear");
   e = cudaMemsetAsync(fb.err, 0, sizeof(unsigned), s);
   if (e) return fail(e, "err clear");
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   init_perm<<<std::min<int64_t>(grid1(n * T), int64_t(sms) * 16), 256, 0, s>>>(perm, n, T);
   note_launch();
   NodeArr cur = node_arr(fb.node_a, fb.max_nodes), nxt = node_arr(fb.node_b, fb.max_nodes);
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   root_nodes<<<1, 64, 0, s>>>(cur, n, T, leaf, leaf_flag, jt, roots_with_split);
   note_launch();
   int64_t cnt = int64_t(T) * roots_with_split;
@@ -366,6 +368,7 @@ int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t 
   int64_t host_i64[2];
   while (cnt > 0) {
     if (level >= kMaxLevels) {
+      cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
       chunk_leaves<<<grid1(cnt), 256, 0, s>>>(cur, int(cnt), leaf, leaf_flag);
       note_launch();
       break;
@@ -378,6 +381,7 @@ int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t 
       }
       rep_dev = fb.replay_dev + 6 * lvl_off[level];
     }
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     pick_pivots<<<grid1(cnt), 256, 0, s>>>(cur, int(cnt), n, seed, level, perm, rep_dev, fb.child_cnt, fb.err, jt);
     note_launch();
     if ((e = exclusive_scan_i32(fb.child_cnt, fb.tile_off, cnt, fb.dev_i64, fb.scan_tmp, s))) return fail(e, "tile scan");
@@ -388,18 +392,23 @@ int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t 
       if (err) *err = "forest tile overflow";
       return KNNG_E_ARGS;
     }
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     side_kernel<<<unsigned(tiles), 256, 0, s>>>(codes, d, perm, cur, int(cnt), fb.tile_off, fb.side, fb.tile_left);
     note_launch();
     if ((e = exclusive_scan_i32(fb.tile_left, fb.tile_left_off, tiles, nullptr, fb.scan_tmp, s))) return fail(e, "left scan");
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     scatter_kernel<<<unsigned(tiles), 256, 0, s>>>(perm, fb.perm_tmp, cur, int(cnt), fb.tile_off, fb.side,
                                                    fb.tile_left, fb.tile_left_off);
     note_launch();
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     copyback_kernel<<<unsigned(tiles), 256, 0, s>>>(perm, fb.perm_tmp, cur, int(cnt), fb.tile_off);
     note_launch();
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     children_count<<<grid1(cnt), 256, 0, s>>>(cur, int(cnt), leaf, fb.tile_off, fb.tile_left, fb.tile_left_off,
                                               leaf_flag, fb.child_cnt);
     note_launch();
     if ((e = exclusive_scan_i32(fb.child_cnt, fb.child_cnt, cnt, fb.dev_i64 + 1, fb.scan_tmp, s))) return fail(e, "child scan");
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     children_emit<<<grid1(cnt), 256, 0, s>>>(cur, int(cnt), leaf, fb.tile_off, fb.tile_left, fb.tile_left_off,
                                              fb.child_cnt, nxt, fb.max_nodes, fb.err);
     note_launch();

@@ -231,6 +231,7 @@ cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm,
   // two CTAs per SM at most: 2 x 128 TMEM columns of the 512, and ~65 KB shared memory each
   const int64_t blocks = std::min<int64_t>(pairs, int64_t(num_sms) * 2);
   if (blocks <= 0) return cudaSuccess;
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   leaf_gram_tc<<<unsigned(blocks), kTcThreads, smem, s>>>(codes, d, perm, leaf_start, nleaves, total, gram, err);
   note_launch();
   return cudaGetLastError();

@@ -396,15 +396,18 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
   const int64_t tn = int64_t(T) * n;
   const unsigned g = unsigned(std::min<int64_t>(grid1(tn), int64_t(sms) * 32));
   int32_t* leaf_start = ib.leaf_idx + tn;  // second half of the leaf_idx allocation
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   flags_to_i32<<<g, 256, 0, s>>>(leaf_flag, ib.leaf_idx, tn);
   note_launch();
   if ((e = exclusive_scan_i32(ib.leaf_idx, ib.leaf_idx, tn, ib.dev_i64, ib.scan_tmp, s))) return fail(e, "leaf scan");
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   leaf_starts<<<g, 256, 0, s>>>(leaf_flag, ib.leaf_idx, tn, leaf_start);
   note_launch();
   int64_t nleaves = 0;
   if ((e = cudaMemcpyAsync(&nleaves, ib.dev_i64, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "leaf count");
   if ((e = cudaStreamSynchronize(s))) return fail(e, "leaf table");
   if (leaves_out) *leaves_out = nleaves;
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   leaf_fill<<<unsigned(std::min<int64_t>(grid1(nleaves), int64_t(sms) * 32)), 256, 0, s>>>(
       leaf_start, nleaves, tn, n, perm, ib.pos, ib.leaf_lo, ib.leaf_sz);
   note_launch();
@@ -417,11 +420,13 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
     const size_t smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
     if ((e = cudaFuncSetAttribute(leaf_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))))
       return fail(e, "gram smem");
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     leaf_gram<<<unsigned(std::min<int64_t>(nleaves, int64_t(sms) * 24)), kGramThreads, smem, s>>>(
         codes, d, perm, leaf_start, nleaves, tn, ib.gram);
     note_launch();
   }
   if ((e = cudaMemsetAsync(ib.dev_i64 + 1, 0, 8, s))) return fail(e, "fix count");
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   init_merge<<<unsigned(std::min<int64_t>((n + 7) / 8, int64_t(sms) * 16)), 256, 0, s>>>(
       n, T, K, perm, ib.pos, ib.leaf_lo, ib.leaf_sz, ib.gram, ids, scores, ib.fix_rows, ib.dev_i64 + 1);
   note_launch();
@@ -436,6 +441,7 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
     return KNNG_E_TIMEOUT;
   }
   if (nfix > 0) {
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     init_fixup<<<grid1(nfix, 64), 64, 0, s>>>(codes, d, n, K, seed, ib.fix_rows, nfix, ids, scores, jt);
     note_launch();
     if ((e = cudaGetLastError())) return fail(e, "init fixup");
@@ -446,6 +452,7 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
 cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int K, uint32_t seed, const JobTable& jt,
                                int32_t* ids, int32_t* scores, int num_sms, cudaStream_t s) {
   const int64_t blocks = std::min<int64_t>((n_total + 7) / 8, int64_t(num_sms) * 16);
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   init_random_kernel<<<unsigned(blocks), 256, 0, s>>>(codes, d, n_total, K, seed, jt, ids, scores);
   note_launch();
   return cudaGetLastError();
@@ -456,6 +463,7 @@ cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, 
   const int64_t tot = n * k_eval;
   if (tot <= 0) return cudaSuccess;
   const JobTable none{};
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   export_kernel<<<unsigned(std::min<int64_t>(grid1(tot), 4096)), 256, 0, s>>>(ids, scores, n, K, k_eval, id_map,
                                                                                knns, dists, jt ? *jt : none);
   note_launch();

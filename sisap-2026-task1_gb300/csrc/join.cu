@@ -590,6 +590,7 @@ cudaError_t join_prepare(int K, int R, int d, int ctas_per_sm, int cblock) {
 
 cudaError_t launch_stop_check(const JobTable& jt, const JoinCtl& ctl, int K, int iter, int out_buf, float stop_rate,
                               float diff_tol, cudaStream_t s) {
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   stop_check_kernel<<<1, 256, 0, s>>>(jt, ctl, K, iter, out_buf, stop_rate, diff_tol);
   note_launch();
   return cudaGetLastError();
@@ -609,6 +610,7 @@ cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, 
       return;
     }
     const int64_t blocks = std::min<int64_t>(n, int64_t(num_sms) * max_per_sm);
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     kern<<<unsigned(blocks), kThreads, smem, s>>>(codes, sketch, n, d, K, R, ids_in, scores_in, ids_out, scores_out,
                                                   row_order, counters, jt ? *jt : no_jobs, ctl ? *ctl : no_ctl);
     e = cudaGetLastError();

@@ -85,6 +85,7 @@ cudaError_t launch_quantize(const float* x, int64_t n, int d, int quant_mode, in
   int64_t want = (chunks + 255) / 256;
   int64_t cap = int64_t(sms) * 8;
   int blocks = int(want < cap ? want : cap);
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   quantize_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(x), chunks, quant_mode,
                                          reinterpret_cast<uint4*>(codes), sketch);
   note_launch();

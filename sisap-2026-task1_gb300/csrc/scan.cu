@@ -94,15 +94,18 @@ cudaError_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, int64
   }
   const int64_t nb = nblocks(n);
   if (nb == 1) {
+    cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     block_scan<<<1, kThreads, 0, s>>>(in, n, nullptr, out, total);
     note_launch();
     return cudaGetLastError();
   }
   int32_t* sums = static_cast<int32_t*>(tmp);
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   block_sums<<<unsigned(nb), kThreads, 0, s>>>(in, n, sums);
   note_launch();
   KNNG_CUDA_TRY(cudaGetLastError());
   KNNG_CUDA_TRY(exclusive_scan_i32(sums, sums, nb, nullptr, sums + nb, s));
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   block_scan<<<unsigned(nb), kThreads, 0, s>>>(in, n, sums, out, total);
   note_launch();
   return cudaGetLastError();
