@@ -30,6 +30,24 @@ std::atomic<int64_t> g_launches{0};
 }
 std::mutex g_capture_mu;
 int64_t launches() { return g_launches.load(std::memory_order_relaxed); }
+
+namespace {
+std::mutex g_attr_mu;
+std::map<const void*, size_t> g_attr_max;
+}  // namespace
+
+cudaError_t ensure_smem_attr(const void* func, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_attr_mu);
+  size_t& cur = g_attr_max[func];
+  if (bytes <= cur) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return e;
+  }
+  cur = bytes;
+  return cudaSuccess;
+}
 void note_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 }  // namespace knng
 

@@ -226,7 +226,7 @@ cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm,
                                 cudaStream_t s) {
   if (d % kChunk != 0) return cudaErrorInvalidValue;
   const size_t smem = 2 * size_t(kStageBytes) + 1024;
-  KNNG_CUDA_TRY(cudaFuncSetAttribute(leaf_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  KNNG_CUDA_TRY(ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram_tc), smem));
   const int64_t pairs = (nleaves + 1) / 2;
   // two CTAs per SM at most: 2 x 128 TMEM columns of the 512, and ~65 KB shared memory each
   const int64_t blocks = std::min<int64_t>(pairs, int64_t(num_sms) * 2);

@@ -418,8 +418,7 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
       return fail(e, "tensor-core gram");
   } else {
     const size_t smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
-    if ((e = cudaFuncSetAttribute(leaf_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))))
-      return fail(e, "gram smem");
+    if ((e = ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram), smem))) return fail(e, "gram smem");
     cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     leaf_gram<<<unsigned(std::min<int64_t>(nleaves, int64_t(sms) * 24)), kGramThreads, smem, s>>>(
         codes, d, perm, leaf_start, nleaves, tn, ib.gram);

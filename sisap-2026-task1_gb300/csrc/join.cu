@@ -539,7 +539,7 @@ cudaError_t max_ctas(size_t smem, int* per_sm_out) {
   cudaError_t e = cudaFuncGetAttributes(&fa, join_kernel<CB, MINB>);  // loads the function
   const char* what = "cudaFuncGetAttributes";
   if (e == cudaSuccess) {
-    e = cudaFuncSetAttribute(join_kernel<CB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    e = ensure_smem_attr(reinterpret_cast<const void*>(join_kernel<CB, MINB>), smem);
     what = "cudaFuncSetAttribute";
   }
   int per_sm = 0;

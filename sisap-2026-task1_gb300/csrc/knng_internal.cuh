@@ -24,6 +24,12 @@ inline bool dim_ok(int d) { return d >= 128 && d <= kMaxDim && d % 128 == 0; }
 int64_t launches();
 void note_launch(int k = 1);
 
+// Raise a kernel's dynamic shared-memory limit to at least `bytes`.  The
+// attribute belongs to the function (process-wide), not to a launch, so it is
+// only ever raised, under one mutex: a concurrent launch that needs less can
+// never find it lowered under it.
+cudaError_t ensure_smem_attr(const void* func, size_t bytes);
+
 // A batch of independent jobs laid out back to back: job b owns global rows
 // [off[b], off[b] + n[b]) of an N-row problem (N = sum n).  Per-tree arrays are
 // tree-major, [T][N], so tree t of job b is the range t*N + off[b] ... and a

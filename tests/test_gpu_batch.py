@@ -78,3 +78,13 @@ def test_batch_device_inputs_and_no_autotune(knng_mod, datasets, solo):
         res, _ = ctx.build_batch(xs)
     res = [(k.cpu().numpy(), dd.cpu().numpy(), it) for k, dd, it in res]
     _check(res, solo, range(4))
+
+
+def test_batch_mixed_dims_dp4a_gram(knng_mod, datasets, solo):
+    """Concurrent dimension groups launch the same kernels with different dynamic
+    shared-memory sizes (the dp4a Gram's grows with d); each must keep working."""
+    with knng_mod.Context(gram_mode=knng_mod.GRAM_DP4A, k_build=20, rerank_mult=3) as small:
+        small.build_batch(datasets[:3])  # smaller join tables first
+    with knng_mod.Context(gram_mode=knng_mod.GRAM_DP4A) as ctx:
+        res, _ = ctx.build_batch(datasets)
+    _check(res, solo, range(len(datasets)))
