@@ -90,6 +90,8 @@ struct knng_ctx {
   cudaEvent_t ev[8] = {};
   cudaEvent_t jev[2] = {};
   cudaEvent_t bev = nullptr;  // start of a batch (all dimension groups wait on it)
+  cudaStream_t copy_stream = nullptr;  // host-input chunks, overlapped with quantisation
+  cudaEvent_t copied[2] = {}, freed[2] = {};
   cudaEvent_t itev[kMaxIterEvents] = {};
   std::string last_error;
   DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs;
@@ -229,19 +231,26 @@ int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_devic
     e = launch_quantize(static_cast<const float*>(rows), n, d, c->prm.quant_mode, codes, sketch, c->stream);
     return e ? cuda_fail(c, e, "quantize") : KNNG_OK;
   }
-  // Host rows: stream fixed-size chunks through two staging buffers so the
-  // copy of chunk k+1 overlaps the quantisation of chunk k (the reference
-  // streams 2.2M-row hyperslabs the same way, src/main.cpp:165-177).
+  // Host rows: stream fixed-size chunks through two staging buffers; the copy
+  // of chunk k+1 (copy stream) overlaps the quantisation of chunk k (context
+  // stream), ordered by per-buffer events (the reference streams 2.2M-row
+  // hyperslabs the same way, src/main.cpp:165-177).
   const size_t chunk_bytes = size_t(kStageRows) * d * 4;
   if ((e = c->staging.ensure(2 * chunk_bytes))) return cuda_fail(c, e, "staging allocation");
   const float* src = static_cast<const float*>(rows);
+  if ((e = cudaEventRecord(c->freed[0], c->stream)) || (e = cudaEventRecord(c->freed[1], c->stream)))
+    return cuda_fail(c, e, "staging events");
   for (int64_t off = 0, k = 0; off < n; off += kStageRows, ++k) {
     const int64_t m = std::min<int64_t>(kStageRows, n - off);
-    float* stage = c->staging.as<float>((k & 1) * chunk_bytes);
-    if ((e = cudaMemcpyAsync(stage, src + off * d, size_t(m) * d * 4, cudaMemcpyHostToDevice, c->stream)))
+    const int b = int(k & 1);
+    float* stage = c->staging.as<float>(b * chunk_bytes);
+    if ((e = cudaStreamWaitEvent(c->copy_stream, c->freed[b], 0)) ||
+        (e = cudaMemcpyAsync(stage, src + off * d, size_t(m) * d * 4, cudaMemcpyHostToDevice, c->copy_stream)) ||
+        (e = cudaEventRecord(c->copied[b], c->copy_stream)) || (e = cudaStreamWaitEvent(c->stream, c->copied[b], 0)))
       return cuda_fail(c, e, "input copy");
     if ((e = launch_quantize(stage, m, d, c->prm.quant_mode, codes + off * d, sketch + off * W, c->stream)))
       return cuda_fail(c, e, "quantize");
+    if ((e = cudaEventRecord(c->freed[b], c->stream))) return cuda_fail(c, e, "staging events");
   }
   return KNNG_OK;
 }
@@ -592,10 +601,16 @@ int knng_create(knng_ctx** out, const knng_params* p) {
       knng_destroy(c);
       return KNNG_E_CUDA;
     }
-  if ((e = cudaEventCreate(&c->bev))) {
+  if ((e = cudaEventCreate(&c->bev)) || (e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking))) {
     knng_destroy(c);
     return KNNG_E_CUDA;
   }
+  for (int k = 0; k < 2; ++k)
+    if ((e = cudaEventCreateWithFlags(&c->copied[k], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&c->freed[k], cudaEventDisableTiming))) {
+      knng_destroy(c);
+      return KNNG_E_CUDA;
+    }
   for (DevBuf* b : c->buffers()) b->s = c->stream;
   // resolve the join kernels' launch attributes now, outside any capture
   for (int d : {128, 256, 384, 512, 640, 768, 896, 1024})
@@ -618,6 +633,11 @@ void knng_destroy(knng_ctx* c) {
   for (auto& ev : c->itev)
     if (ev) cudaEventDestroy(ev);
   if (c->bev) cudaEventDestroy(c->bev);
+  for (int k = 0; k < 2; ++k) {
+    if (c->copied[k]) cudaEventDestroy(c->copied[k]);
+    if (c->freed[k]) cudaEventDestroy(c->freed[k]);
+  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : c->jev)
