@@ -108,7 +108,7 @@ struct knng_ctx {
 
 namespace {
 
-constexpr int64_t kStageRows = 1 << 16;  // host-input rows per H2D chunk
+constexpr int64_t kStageRows = 1 << 20;  // host-input rows per H2D chunk (fewer, larger copies)
 
 int set_error(knng_ctx* c, int status, const std::string& msg) {
   if (c) c->last_error = msg;
@@ -235,13 +235,14 @@ int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_devic
   // of chunk k+1 (copy stream) overlaps the quantisation of chunk k (context
   // stream), ordered by per-buffer events (the reference streams 2.2M-row
   // hyperslabs the same way, src/main.cpp:165-177).
-  const size_t chunk_bytes = size_t(kStageRows) * d * 4;
+  const int64_t chunk_rows = std::min<int64_t>(kStageRows, n);
+  const size_t chunk_bytes = size_t(chunk_rows) * d * 4;
   if ((e = c->staging.ensure(2 * chunk_bytes))) return cuda_fail(c, e, "staging allocation");
   const float* src = static_cast<const float*>(rows);
   if ((e = cudaEventRecord(c->freed[0], c->stream)) || (e = cudaEventRecord(c->freed[1], c->stream)))
     return cuda_fail(c, e, "staging events");
-  for (int64_t off = 0, k = 0; off < n; off += kStageRows, ++k) {
-    const int64_t m = std::min<int64_t>(kStageRows, n - off);
+  for (int64_t off = 0, k = 0; off < n; off += chunk_rows, ++k) {
+    const int64_t m = std::min<int64_t>(chunk_rows, n - off);
     const int b = int(k & 1);
     float* stage = c->staging.as<float>(b * chunk_bytes);
     if ((e = cudaStreamWaitEvent(c->copy_stream, c->freed[b], 0)) ||
@@ -746,7 +747,7 @@ int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on
   b += std::max(f, in) + 64 * 1024;
   b += size_t(n) * q.k_eval * 8;                                   // export buffer
   b += size_t(q.max_iterations + 1) * 64 * 8 + 4096;               // control block (per job, bounded)
-  if (!rows_on_device) b += size_t(2) * kStageRows * d * 4;        // host-input staging
+  if (!rows_on_device) b += size_t(2) * std::min<int64_t>(kStageRows, n) * d * 4;  // host-input staging
   return int64_t(b) + (int64_t(1) << 24);                          // pool rounding slack
 }
 
