@@ -108,7 +108,7 @@ struct knng_ctx {
 
 namespace {
 
-constexpr int64_t kStageRows = 1 << 20;  // host-input rows per H2D chunk (fewer, larger copies)
+constexpr int64_t kStageRows = 1 << 16;  // host-input rows per H2D chunk (256 MB at d = 1024)
 
 int set_error(knng_ctx* c, int status, const std::string& msg) {
   if (c) c->last_error = msg;
