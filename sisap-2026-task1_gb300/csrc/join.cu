@@ -236,9 +236,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
           if (n2 >= 0 && n2 < n && n2 != i) sl = table_insert(key, mask, n2, 0u);
           cand_slot[j] = int16_t(sl);
           if (sl >= 0) {
-            // an earlier occurrence already recorded: nothing to do (no atomic);
-            // among racing first occurrences exactly one sees the untouched mark
-            if ((meta[sl] & kFirstMask) > uint32_t(j)) first = atomicMin(&meta[sl], uint32_t(j)) == kFirstMask;
+            first = atomicMin(&meta[sl], uint32_t(j)) == kFirstMask;
             ++local_cnt;
           }
         }
@@ -281,12 +279,9 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     }
     __syncthreads();
     // ---- D  histogram over occurrences, threshold
-    for (int jb = 0; jb < KK; jb += kThreads) {  // warp-uniform trip count for the match
-      const int j = jb + tid;
-      const int sl = j < KK ? int(cand_slot[j]) : -1;
-      const int h = sl >= 0 ? int((meta[sl] >> 16) & 0x7ffu) : -1;
-      const unsigned same = __match_any_sync(0xffffffffu, h);  // lanes with the same h add once
-      if (h >= 0 && (__ffs(same) - 1) == lane) atomicAdd(&hist[h], unsigned(__popc(same)));
+    for (int j = tid; j < KK; j += kThreads) {
+      const int sl = cand_slot[j];
+      if (sl >= 0) atomicAdd(&hist[(meta[sl] >> 16) & 0x7ffu], 1u);
     }
     __syncthreads();
     const int cnt = s_cnt;
