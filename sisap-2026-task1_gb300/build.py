@@ -4,8 +4,9 @@
 
 Each csrc/*.cu compiles to _build/<name>.o in parallel (one -gencode, sm_103a
 only), then nvcc links libknng.so next to this file; host/*.cpp link into
-knng_main against it (rpath $ORIGIN).  Targets are rebuilt only when a source
-or header is newer.
+knng_main against it (rpath $ORIGIN), with zlib (deflate-compressed HDF5
+input) when the host has its header and library.  Targets are rebuilt only
+when a source or header is newer.
 """
 from __future__ import annotations
 
@@ -14,6 +15,7 @@ import glob
 import os
 import subprocess
 import sys
+import tempfile
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
@@ -48,6 +50,16 @@ def _run(cmd):
     return r
 
 
+def _zlib_flags():
+    """["-DKNNG_HAVE_ZLIB", "-lz"] when a zlib program compiles and links here."""
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "z.cpp")
+        with open(src, "w") as f:
+            f.write("#include <zlib.h>\nint main() { return zlibVersion()[0] == 0; }\n")
+        r = subprocess.run(["g++", src, "-o", os.path.join(d, "z"), "-lz"], capture_output=True)
+    return ["-DKNNG_HAVE_ZLIB", "-lz"] if r.returncode == 0 else []
+
+
 def build(force=False, verbose=False):
     os.makedirs(OUT, exist_ok=True)
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
@@ -67,8 +79,9 @@ def build(force=False, verbose=False):
     host_srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
     host_hdrs = glob.glob(os.path.join(HOST, "*.h"))
     if host_srcs and (force or _newer(CLI, host_srcs + host_hdrs + [LIB])):
-        _run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include")] + host_srcs +
-             ["-o", CLI, "-L", PKG, "-lknng", "-Wl,-rpath,$ORIGIN"])
+        z = _zlib_flags()
+        _run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include")] + z[:1] +
+             host_srcs + ["-o", CLI, "-L", PKG, "-lknng", "-Wl,-rpath,$ORIGIN"] + z[1:])
     return LIB
 
 

@@ -48,11 +48,16 @@ def write(path, datasets=None, str_attrs=None, float_attrs=None):
 
 
 def read(path, mmap=True):
-    """Return (datasets, attrs) from a container file; datasets are memory-mapped."""
+    """Return (datasets, attrs) from a container or an HDF5 file (told apart by
+    the signature; HDF5 goes through hdf5read).  Datasets are memory-mapped
+    unless ``mmap`` is False."""
     datasets, attrs = {}, {}
     with open(path, "rb") as f:
         if f.read(8) != MAGIC:
-            raise ValueError(f"{path}: not a knng container file")
+            import hdf5read
+
+            ds, at = hdf5read.read(path)
+            return ({k: np.array(v) for k, v in ds.items()} if not mmap else ds), at
         while True:
             hdr = f.read(8)
             if len(hdr) < 8:

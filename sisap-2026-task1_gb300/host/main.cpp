@@ -13,6 +13,12 @@
 //   --k-build K --k-eval k --trees T --leaf L --rerank M --max-iter I
 //   --quant trunc|round --join jacobi|inplace --order leaf|natural
 //   --device D --stats-json FILE
+//   --output-format hdf5|knng   (result file format; hdf5 by default)
+// and an inspection mode that needs no GPU:
+//   knng_main --h5dump FILE [DATASET]   prints the file's datasets and root
+//   attributes (and DATASET's values as float32) as one JSON object;
+//   knng_main --convert SRC DST [--output-format hdf5|knng]   rewrites a
+//   result file (knns, dists, attributes) in the other format.
 #include <sys/stat.h>
 
 #include <chrono>
@@ -25,9 +31,61 @@
 #include <vector>
 
 #include "h5io.h"
+#include "hdf5.h"
 #include "knng.h"
 
 namespace {
+
+std::string json_str(const std::string& s) {
+  std::string o = "\"";
+  for (unsigned char ch : s) {
+    if (ch == '"' || ch == '\\') {
+      o += '\\';
+      o += char(ch);
+    } else if (ch < 0x20) {
+      char b[8];
+      std::snprintf(b, sizeof b, "\\u%04x", ch);
+      o += b;
+    } else {
+      o += char(ch);
+    }
+  }
+  return o + "\"";
+}
+
+int h5dump(const std::string& path, const std::string& dataset) {
+  try {
+    std::string out = "{\"datasets\": [";
+    const auto ds = knngio::h5::list_datasets(path);
+    for (size_t i = 0; i < ds.size(); ++i) {
+      out += (i ? ", " : "") + std::string("{\"name\": ") + json_str(ds[i].name) +
+             ", \"class\": " + std::to_string(ds[i].type_class) + ", \"size\": " + std::to_string(ds[i].type_size) +
+             ", \"little_endian\": " + (ds[i].little_endian ? "true" : "false") +
+             ", \"signed\": " + (ds[i].is_signed ? "true" : "false") + ", \"dims\": [";
+      for (size_t k = 0; k < ds[i].dims.size(); ++k) out += (k ? ", " : "") + std::to_string(ds[i].dims[k]);
+      out += "]}";
+    }
+    out += "], \"attrs\": {";
+    const auto at = knngio::h5::read_attributes(path, "/");
+    for (size_t i = 0; i < at.size(); ++i) out += (i ? ", " : "") + json_str(at[i].first) + ": " + json_str(at[i].second);
+    out += "}";
+    if (!dataset.empty()) {
+      const std::vector<float> v = knngio::h5::read_float(path, dataset, nullptr);
+      out += ", \"values\": [";
+      char b[32];
+      for (size_t i = 0; i < v.size(); ++i) {
+        std::snprintf(b, sizeof b, "%s%.9g", i ? ", " : "", double(v[i]));
+        out += b;
+      }
+      out += "]";
+    }
+    std::cout << out << "}\n";
+    return 0;
+  } catch (const std::exception& e) {
+    std::cerr << "[FATAL] " << e.what() << "\n";
+    return -1;
+  }
+}
 
 bool take_int(const std::string& a, const char* flag, int argc, char** argv, int& i, int& out) {
   if (a != flag || i + 1 >= argc) return false;
@@ -44,13 +102,32 @@ std::string fmt_params(const knng_params& p) {
 
 }  // namespace
 
+int convert(const std::string& src, const std::string& dst, knngio::Format format) {
+  try {
+    const knngio::Result r = knngio::read_result(src);
+    const knngio::Output o{r.knns.data(), r.dists.data(), r.rows, r.cols, r.algo, r.task, r.params, r.buildtime,
+                           r.querytime};
+    knngio::write_result(dst, o, format);
+    return 0;
+  } catch (const std::exception& e) {
+    std::cerr << "[FATAL] " << e.what() << "\n";
+    return -1;
+  }
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 3 && std::string(argv[1]) == "--h5dump") return h5dump(argv[2], argc >= 4 ? argv[3] : "");
+  if (argc >= 4 && std::string(argv[1]) == "--convert") {
+    const bool knng = argc >= 6 && std::string(argv[4]) == "--output-format" && std::string(argv[5]) == "knng";
+    return convert(argv[2], argv[3], knng ? knngio::Format::kContainer : knngio::Format::kHdf5);
+  }
   const auto global_start = std::chrono::steady_clock::now();
   std::cout << "==================================================\n";
   std::cout << "   KNNG GB300 ENGINE: kNN-GRAPH BUILD ON ONE GPU   \n";
   std::cout << "==================================================\n";
 
   std::string filename, task_name = "task1", stats_json;
+  knngio::Format out_format = knngio::Format::kHdf5;
   knng_params prm;
   knng_default_params(&prm);
   for (int i = 1; i < argc; ++i) {
@@ -68,6 +145,8 @@ int main(int argc, char** argv) {
       prm.join_mode = std::string(argv[++i]) == "inplace" ? KNNG_JOIN_INPLACE : KNNG_JOIN_JACOBI;
     } else if (a == "--order" && i + 1 < argc) {
       prm.row_order = std::string(argv[++i]) == "natural" ? KNNG_ORDER_NATURAL : KNNG_ORDER_LEAF;
+    } else if (a == "--output-format" && i + 1 < argc) {
+      out_format = std::string(argv[++i]) == "knng" ? knngio::Format::kContainer : knngio::Format::kHdf5;
     } else if (a == "--stats-json" && i + 1 < argc) {
       stats_json = argv[++i];
     } else if (a == "--dataset" && i + 1 < argc) {
@@ -129,7 +208,7 @@ int main(int argc, char** argv) {
   try {
     knngio::Output o{knns.data(), dists.data(), n, prm.k_eval, "knng GB300", task_name, fmt_params(prm),
                      float(stats.build_s), 0.0f};
-    knngio::write_result(out_filename, o);
+    knngio::write_result(out_filename, o, out_format);
   } catch (const std::exception& e) {
     std::cerr << "[FATAL] File Write Error: " << e.what() << "\n";
     return -1;
