@@ -367,7 +367,7 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     x = synth.mixture_torch(n, d, centres, seed=1000 * 2 + rank, device=dev)
     torch.cuda.synchronize()
-    prm = knng.params(device=local, gram_mode=GRAM[args.gram])
+    prm = knng.params(device=local, gram_mode=GRAM[args.gram], join_cache=args.join_cache)
     ctx = knng.Context(prm)
     knns = torch.empty((n, prm.k_eval), dtype=torch.int32, device=dev)
     dists = torch.empty((n, prm.k_eval), dtype=torch.float32, device=dev)
@@ -419,7 +419,13 @@ def run_gpu(args):
     alg_bytes = []
     for i in range(it):
         rows_b = n * (K * 8 + K * K * 4 + d + W8 + K * 8)  # own list, 2-hop ids, own row+sketch, list write
-        alg_bytes.append(rows_b + last.join_candidates[i] * W8 + last.join_dots[i] * d)
+        # candidate cache: this iteration's distinct candidates written (6 B each, at most 1536 per row),
+        # the previous iteration's read back
+        cache_b = 0
+        if prm.join_cache:
+            wr = min(last.join_distinct[i], 1536 * n)
+            cache_b = 6 * (wr + (min(last.join_distinct[i - 1], 1536 * n) if i else 0))
+        alg_bytes.append(rows_b + last.join_candidates[i] * W8 + last.join_dots[i] * d + cache_b)
     peak, peak_kind = load_peaks()
     achieved = sum(alg_bytes) / (sum(join_ms) * 1e-3) / 1e9 if it else 0.0
     roofline = {"kernel": "join_kernel (NN-Descent iteration)", "bound": "hbm", "achieved": achieved,
@@ -452,6 +458,7 @@ def run_gpu(args):
                        "k_build": K, "trees": prm.num_trees, "leaf": prm.leaf_size, "rerank": prm.rerank_mult,
                        "join": "jacobi" if prm.join_mode == 0 else "inplace",
                        "leaf_gram": "tcgen05 bf16" if prm.gram_mode == 1 else "dp4a",
+                       "candidate_cache": bool(prm.join_cache),
                        "l2": "inputs (n x d float32) far larger than L2; no flush",
                        "parallelism": f"replicas x{ws}"},
             "build_s": last.build_s, "step_s": last.device_s, "iterations": it,
@@ -476,6 +483,8 @@ def main():
     ap.add_argument("--config", default="full", choices=sorted(CONFIGS) + ["batched", "serving"])
     ap.add_argument("--gram", default="tc", choices=["tc", "dp4a"],
                     help="leaf Gram: tcgen05 bf16 tensor cores or dp4a")
+    ap.add_argument("--join-cache", type=int, default=1, choices=[0, 1],
+                    help="per-row candidate cache in the NN-Descent join (identical results; 1 = default)")
     ap.add_argument("--serve-jobs", type=int, default=32)
     ap.add_argument("--slots", type=int, default=3)
     ap.add_argument("--recall-rows", type=int, default=10_000)

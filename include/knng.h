@@ -68,6 +68,10 @@ typedef struct knng_params {
   int gram_mode;         /* leaf Gram: KNNG_GRAM_DP4A or KNNG_GRAM_TCGEN05 (bf16 tensor cores) */
   int init_mode;         /* KNNG_INIT_FOREST (src/main.cpp) or KNNG_INIT_RANDOM, the archived
                             variant archive/nndescent_optimized.cpp:97-118 (needs n > k_build) */
+  int join_cache;        /* 1: each row keeps its previous iteration's distinct candidates with
+                            their Hamming scores and known rejections (n * 9.2 KB of device
+                            memory), so later iterations skip most sketch and row gathers;
+                            results are identical either way.  0: no cache. */
 } knng_params;
 
 /* Per-build timings and convergence record (seconds, device-timed). */
@@ -85,12 +89,14 @@ typedef struct knng_stats {
   int64_t leaves;
   double device_s;        /* first to last device event of the call */
   double join_ms[64];     /* device time of each NN-Descent launch */
-  int64_t join_candidates[64]; /* sketch candidates scored per iteration */
+  int64_t join_candidates[64]; /* sketches scored per iteration (distinct candidates without a
+                                  cached score) */
   int64_t join_dots[64];  /* int8 rows reranked per iteration */
   int64_t kernel_launches;/* libknng kernels launched by the call */
   int join_ctas_per_sm;   /* autotuned join configuration used */
   int join_cblock;
   int graph_used;         /* NN-Descent phase ran as a CUDA graph */
+  int64_t join_distinct[64]; /* distinct two-hop candidates per iteration (all rows) */
 } knng_stats;
 
 /* One job of a batch (knng_build_batch).  Inputs as for knng_build; status

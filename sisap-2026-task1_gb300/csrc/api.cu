@@ -94,7 +94,7 @@ struct knng_ctx {
   cudaEvent_t copied[2] = {}, freed[2] = {};
   cudaEvent_t itev[kMaxIterEvents] = {};
   std::string last_error;
-  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs;
+  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs, cache;
   // join phase captured as a CUDA graph, reused while the launch key matches
   cudaGraphExec_t join_graph = nullptr;
   std::vector<uintptr_t> join_graph_key;
@@ -102,7 +102,7 @@ struct knng_ctx {
   std::map<std::pair<int, int>, std::pair<int, int>> tuned;
   std::vector<knng_ctx*> subs;  // contexts of the second and later dimension groups of a batch
   std::vector<DevBuf*> buffers() {
-    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs};
+    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs, &cache};
   }
 };
 
@@ -136,6 +136,7 @@ int check_params(knng_ctx* c, const knng_params& p) {
   if (p.row_order != KNNG_ORDER_NATURAL && p.row_order != KNNG_ORDER_LEAF) return set_error(c, KNNG_E_ARGS, "bad row_order");
   if (p.gram_mode != KNNG_GRAM_DP4A && p.gram_mode != KNNG_GRAM_TCGEN05) return set_error(c, KNNG_E_ARGS, "bad gram_mode");
   if (p.init_mode != KNNG_INIT_FOREST && p.init_mode != KNNG_INIT_RANDOM) return set_error(c, KNNG_E_ARGS, "bad init_mode");
+  if (p.join_cache != 0 && p.join_cache != 1) return set_error(c, KNNG_E_ARGS, "join_cache must be 0 or 1");
   return KNNG_OK;
 }
 
@@ -318,7 +319,7 @@ cudaError_t join_phase(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int
                 : cudaEventRecord(c->itev[2 * it], c->stream);
     if (e) return (*step = "iteration start event", e);
     if ((e = launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[cur],
-                         scs[cur], ids[nxt], scs[nxt], order, counters + 3 * it, c->num_sms, c->stream, &jt, &ctl,
+                         scs[cur], ids[nxt], scs[nxt], order, counters + 4 * it, c->num_sms, c->stream, &jt, &ctl,
                          cfg.first, cfg.second)))
       return (*step = "join launch", e);
     e = capture ? cudaEventRecordWithFlags(c->itev[2 * it + 1], c->stream, cudaEventRecordExternal)
@@ -368,7 +369,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   };
   const size_t o_off = take(jb * 4), o_n = take(jb * 4), o_upd = take(jb * 8), o_done = take(jb * 4),
                o_prev = take(jb * 4), o_iters = take(jb * 4), o_flags = take(16), o_log = take(size_t(MI + 1) * jb * 8),
-               o_cnt = take(size_t(MI + 1) * 3 * 8);
+               o_cnt = take(size_t(MI + 1) * 4 * 8);
   if ((e = c->jobs.ensure(o))) return cuda_fail(c, e, "job table allocation");
   cudaStream_t str = c->stream;
   if ((e = cudaMemsetAsync(c->jobs.p, 0, o, str)) ||
@@ -388,7 +389,21 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   ctl.all_done = c->jobs.as<int>(o_flags);
   ctl.final_buf = c->jobs.as<int>(o_flags) + 1;
   ctl.upd_log = c->jobs.as<long long>(o_log);
-  unsigned long long* tune_counters = ctl.counters + 3 * MI;
+  ctl.cache_ids = nullptr;
+  ctl.cache_hr = nullptr;
+  ctl.cache_cnt = nullptr;
+  ctl.cache_cap = 0;
+  if (p.join_cache && MI > 0) {
+    if ((e = c->cache.ensure(cache_bytes(N)))) return cuda_fail(c, e, "candidate cache allocation");
+    char* cp = c->cache.as<char>();
+    ctl.cache_ids = reinterpret_cast<int32_t*>(cp);
+    cp += (size_t(N) * kCacheCap * 4 + 255) & ~size_t(255);
+    ctl.cache_hr = reinterpret_cast<uint16_t*>(cp);
+    cp += (size_t(N) * kCacheCap * 2 + 255) & ~size_t(255);
+    ctl.cache_cnt = reinterpret_cast<int*>(cp);
+    ctl.cache_cap = kCacheCap;
+  }
+  unsigned long long* tune_counters = ctl.counters + 4 * MI;
   int32_t* ids[2] = {c->graph.as<int32_t>(0), c->graph.as<int32_t>(nk * 8)};
   int32_t* scs[2] = {c->graph.as<int32_t>(nk * 4), c->graph.as<int32_t>(nk * 12)};
 
@@ -418,6 +433,9 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   const int32_t* order = (p.row_order == KNNG_ORDER_LEAF && !random_init) ? c->perm.as<int32_t>() : nullptr;
   const std::pair<int, int> cfg = autotune_join(c, N, d, ids, scs, order, tune_counters);
   cudaEventRecord(c->ev[3], str);
+  // every row starts the phase with an empty candidate cache
+  if (ctl.cache_cnt && (e = cudaMemsetAsync(ctl.cache_cnt, 0, size_t(N) * 4, str)))
+    return cuda_fail(c, e, "candidate cache reset");
   // NN-Descent, captured once per launch key and replayed
   bool graph_used = false;
   if ((e = join_prepare(K, K * p.rerank_mult, d, cfg.first, cfg.second)))
@@ -425,7 +443,8 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   const char* step = "";
   if (p.use_graph) {
     const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->sketch.p), uintptr_t(c->graph.p),
-                                        uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(N), uintptr_t(d),
+                                        uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(ctl.cache_ids),
+                                        uintptr_t(N), uintptr_t(d),
                                         uintptr_t(J), uintptr_t(o), uintptr_t(cfg.first), uintptr_t(cfg.second),
                                         uintptr_t(order != nullptr), uintptr_t(p.join_mode), uintptr_t(MI),
                                         uintptr_t(K), uintptr_t(p.rerank_mult)};
@@ -459,7 +478,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   // results of the control block
   std::vector<int> iters(jb);
   std::vector<long long> log(size_t(MI) * jb);
-  std::vector<unsigned long long> cnt(size_t(MI) * 3);
+  std::vector<unsigned long long> cnt(size_t(MI) * 4);
   int flags[2] = {0, 0};
   if ((e = cudaMemcpyAsync(iters.data(), ctl.job_iters, jb * 4, cudaMemcpyDeviceToHost, str)) ||
       (MI && (e = cudaMemcpyAsync(log.data(), ctl.upd_log, log.size() * 8, cudaMemcpyDeviceToHost, str))) ||
@@ -511,8 +530,9 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     for (int b = 0; b < J; ++b) u += log[size_t(it) * J + b];
     S.updates[it] = u;
     S.join_ms[it] = elapsed(c->itev[2 * it], c->itev[2 * it + 1]);
-    S.join_candidates[it] = int64_t(cnt[3 * it + 1]);
-    S.join_dots[it] = int64_t(cnt[3 * it + 2]);
+    S.join_candidates[it] = int64_t(cnt[4 * it + 1]);
+    S.join_dots[it] = int64_t(cnt[4 * it + 2]);
+    S.join_distinct[it] = int64_t(cnt[4 * it + 3]);
   }
   S.forest_levels = levels;
   S.leaves = leaves;
@@ -547,6 +567,7 @@ void knng_default_params(knng_params* p) {
   p->use_graph = 1;
   p->gram_mode = KNNG_GRAM_TCGEN05;
   p->init_mode = KNNG_INIT_FOREST;
+  p->join_cache = 1;
 }
 
 const char* knng_status_string(int s) {
@@ -703,7 +724,7 @@ int knng_join_iter(knng_ctx* c, const int8_t* codes_dev, const uint64_t* sketch_
   cudaError_t e;
   if ((e = c->scalars.ensure(4096))) return cuda_fail(c, e, "scalar allocation");
   unsigned long long* up = c->scalars.as<unsigned long long>(256);
-  if ((e = cudaMemsetAsync(up, 0, 24, c->stream))) return cuda_fail(c, e, "update counter");
+  if ((e = cudaMemsetAsync(up, 0, 32, c->stream))) return cuda_fail(c, e, "update counter");
   const int K = c->prm.k_build;
   if ((e = launch_join(codes_dev, sketch_dev, n, d, K, K * c->prm.rerank_mult, ids_in, scores_in, ids_out,
                        scores_out, nullptr, up, c->num_sms, c->stream)))
@@ -747,6 +768,7 @@ int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on
   b += std::max(f, in) + 64 * 1024;
   b += size_t(n) * q.k_eval * 8;                                   // export buffer
   b += size_t(q.max_iterations + 1) * 64 * 8 + 4096;               // control block (per job, bounded)
+  if (q.join_cache && q.max_iterations > 0) b += cache_bytes(n);   // per-row candidate cache
   if (!rows_on_device) b += size_t(2) * std::min<int64_t>(kStageRows, n) * d * 4;  // host-input staging
   return int64_t(b) + (int64_t(1) << 24);                          // pool rounding slack
 }
@@ -841,6 +863,7 @@ int knng_build_batch(knng_ctx* c, knng_job* jobs, int count, knng_stats* stats) 
       S.join_ms[it] += gs[g].join_ms[it];
       S.join_candidates[it] += gs[g].join_candidates[it];
       S.join_dots[it] += gs[g].join_dots[it];
+      S.join_distinct[it] += gs[g].join_distinct[it];
     }
     S.join_ctas_per_sm = gs[g].join_ctas_per_sm;
     S.join_cblock = gs[g].join_cblock;

@@ -66,15 +66,18 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kGroups = kThreads / 8;  // 8-lane groups per CTA
 constexpr int kHBins = 1025;
+static_assert(kHBins * 4 >= kCacheCap * 2, "the histogram region stages the cached scores");
 constexpr int32_t kEmpty = 0x7fffffff;     // never a valid id (num_trees * n < 2^31)
 constexpr uint32_t kPoolFlag = 0x80000000u; // key bit: id is in the starting list with a real score
-constexpr uint32_t kFirstMask = 0x1fffu;    // meta bits 0..12: first j (8191 = none)
+constexpr uint32_t kFirstMask = 0x1fffu;    // meta bits 0..12: first j (8191 = none); 16..26: Hamming score
+constexpr uint32_t kKnown = 0x80000000u;    // meta bit 31: Hamming score taken from the row's candidate cache
+constexpr uint32_t kRej = 0x40000000u;      // meta bit 30: dot known to be <= the row's pool threshold
 
 struct JoinSmem {
   int K, R, KK, d, W, HT;
   size_t bytes;
   size_t o_code, o_sk, o_slot, o_key, o_meta, o_hist, o_ulist, o_need, o_pkey, o_pid, o_pdot, o_order, o_pool_id,
-      o_pool_sc;
+      o_pool_sc, o_miss;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -96,11 +99,15 @@ __host__ __device__ inline JoinSmem join_smem(int K, int R, int d) {
   s.o_meta = o;    o = align16(o + size_t(s.HT) * 4);
   s.o_hist = o;    o = align16(o + size_t(kHBins) * 4);
   s.o_ulist = o;   o = align16(o + size_t(s.KK) * 2);
+  const size_t u0 = o;  // stage C's miss list shares this region with stages F-H
   s.o_need = o;    o = align16(o + size_t(R) * 2);
   s.o_pkey = o;    o = align16(o + size_t(R) * 4);
   s.o_pid = o;     o = align16(o + size_t(R) * 4);
   s.o_pdot = o;    o = align16(o + size_t(R) * 4);
   s.o_order = o;   o = align16(o + size_t(R) * 2);
+  s.o_miss = u0;  // also stages the row's cached ids (kCacheCap * 4 bytes) before stage B2
+  if (o < align16(u0 + size_t(s.KK) * 2)) o = align16(u0 + size_t(s.KK) * 2);
+  if (o < align16(u0 + size_t(kCacheCap) * 4)) o = align16(u0 + size_t(kCacheCap) * 4);
   s.o_pool_id = o; o = align16(o + size_t(K) * 4);
   s.o_pool_sc = o; o = align16(o + size_t(K) * 4);
   s.bytes = o;
@@ -139,6 +146,26 @@ __device__ __forceinline__ int table_insert(int32_t* key, uint32_t mask, int32_t
   return -1;
 }
 
+// 16-byte global -> shared copy that holds no registers (cp.async, L2 only).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Slot of id (flagged or not), or -1 when the table does not hold it.
+__device__ __forceinline__ int table_find(const int32_t* key, uint32_t mask, int32_t id) {
+  uint32_t s = hash_slot(id, mask);
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    const int32_t k = key[s];
+    if (k == kEmpty) return -1;
+    if ((uint32_t(k) & 0x7fffffffu) == uint32_t(id)) return int(s);
+    s = (s + 1) & mask;
+  }
+  return -1;
+}
+
 template <int CB, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     const int8_t* __restrict__ codes, const uint64_t* __restrict__ sketch, int64_t n, int d, int K, int R,
@@ -155,20 +182,24 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   uint32_t* hist = reinterpret_cast<uint32_t*>(smem + L.o_hist);
   int16_t* ulist = reinterpret_cast<int16_t*>(smem + L.o_ulist);
   int16_t* need = reinterpret_cast<int16_t*>(smem + L.o_need);
+  int16_t* misslist = reinterpret_cast<int16_t*>(smem + L.o_miss);  // shares its region with need..order
+  const int32_t* stage_id = reinterpret_cast<const int32_t*>(smem + L.o_miss);  // stage A..B2, same region
+  const uint16_t* stage_hr = reinterpret_cast<const uint16_t*>(smem + L.o_hist);  // stage A..B2
   uint32_t* pkey = reinterpret_cast<uint32_t*>(smem + L.o_pkey);
   int32_t* pid = reinterpret_cast<int32_t*>(smem + L.o_pid);
   int32_t* pdot = reinterpret_cast<int32_t*>(smem + L.o_pdot);
   uint16_t* order = reinterpret_cast<uint16_t*>(smem + L.o_order);
   int32_t* pool_id = reinterpret_cast<int32_t*>(smem + L.o_pool_id);
   int32_t* pool_sc = reinterpret_cast<int32_t*>(smem + L.o_pool_sc);
-  __shared__ int s_cnt, s_ht, s_gt, s_jcut, s_nu, s_nneed, s_nprom;
+  __shared__ int s_cnt, s_ht, s_gt, s_jcut, s_nu, s_nneed, s_nprom, s_nmiss, s_ccnt;
   __shared__ int32_t s_wsum[kWarps];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, sub = lane & 7, slot8 = lane >> 3;
   const int KK = L.KK, W = L.W, nchunk = d / 16, sk_chunks = W / 2;
   const uint32_t mask = uint32_t(L.HT - 1);
   const bool inplace = ids_out == ids_in;
-  unsigned long long my_updates = 0, my_cands = 0, my_dots = 0;
+  const bool cached = ctl.cache_ids != nullptr;
+  unsigned long long my_updates = 0, my_cands = 0, my_dots = 0, my_distinct = 0;
   int run_job = -1;                 // per-job update count kept by warp 0 lane 0
   unsigned long long run_upd = 0;
 
@@ -193,7 +224,8 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     }
     for (int c = tid; c < nchunk; c += kThreads) my_code[c] = reinterpret_cast<const uint4*>(codes + i * d)[c];
     for (int c = tid; c < sk_chunks; c += kThreads) my_sk[c] = reinterpret_cast<const uint4*>(sketch + i * W)[c];
-    for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;
+    if (!cached)
+      for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;
     for (int t = tid; t < L.HT / 4; t += kThreads) {
       reinterpret_cast<uint4*>(key)[t] = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
       reinterpret_cast<uint4*>(meta)[t] = make_uint4(kFirstMask, kFirstMask, kFirstMask, kFirstMask);
@@ -203,13 +235,33 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       s_nu = 0;
       s_nneed = 0;
       s_nprom = 0;
+      s_ccnt = cached ? ctl.cache_cnt[i] : 0;
     }
     __syncthreads();
+    if (cached) {
+      // stage the row's cache entries into shared memory (ids over the region
+      // of stages F-H, scores over the histogram) while stage B runs; the
+      // rows' cache slices are 16-byte aligned and sized for cache_cap
+      const int cc = min(s_ccnt, ctl.cache_cap);
+      const int n_id = (cc * 4 + 15) / 16, n_hr = (cc * 2 + 15) / 16;
+      const char* gid = reinterpret_cast<const char*>(ctl.cache_ids + i * ctl.cache_cap);
+      const char* ghr = reinterpret_cast<const char*>(ctl.cache_hr + i * ctl.cache_cap);
+      for (int t = tid; t < n_id + n_hr; t += kThreads) {
+        if (t < n_id) cp_async16(smem + L.o_miss + 16 * t, gid + 16 * t);
+        else cp_async16(smem + L.o_hist + 16 * (t - n_id), ghr + 16 * (t - n_id));
+      }
+      cp_async_commit();
+    }
+    int irregular = 0;
     for (int k = tid; k < K; k += kThreads) {
       const int32_t id = pool_id[k];
       if (pool_sc[k] != kScoreMinI && id >= 0 && id < n) table_insert(key, mask, id, kPoolFlag);
+      irregular |= (pool_sc[k] == kScoreMinI) | (k + 1 < K && pool_sc[k] < pool_sc[k + 1]);
     }
-    __syncthreads();
+    // An unscored entry (INT32_MIN, tiny inputs only) can share its id with a
+    // survivor, and an unsorted pool (possible through the stage entry point)
+    // breaks the rank formulas of stage G/H: both take the sequential loop.
+    const bool serial_insert = __syncthreads_or(irregular) != 0;
     // ---- B  (warp per neighbour row, all of the warp's rows loaded first; the
     //         first occurrence to touch a slot appends it to the distinct list)
     {
@@ -249,18 +301,53 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       if (local_cnt) atomicAdd(&s_cnt, local_cnt);
     }
     __syncthreads();
-    // ---- C  Hamming once per distinct id (groups of 8 lanes, 4 in flight)
     const int nu = s_nu;
+    // ---- B2  candidate cache: the row's distinct candidates of the previous
+    //          iteration with their Hamming scores and rejected flags.  Entries
+    //          are only looked up (no slot is added), and a distinct id of this
+    //          iteration without an entry goes to the miss list for stage C.
+    const int16_t* clist = ulist;
+    int ncl = nu;
+    if (cached) {
+      cp_async_wait_all();  // this thread's staging copies, issued in stage A
+      __syncthreads();
+      const int cc = min(s_ccnt, ctl.cache_cap);
+      for (int q = tid; q < cc; q += kThreads) {
+        const int sl = table_find(key, mask, stage_id[q]);
+        if (sl >= 0) {
+          const uint32_t hr = stage_hr[q];
+          meta[sl] = kKnown | ((hr & 1u) ? kRej : 0u) | (uint32_t(hr >> 1) << 16) | (meta[sl] & kFirstMask);
+        }
+      }
+      if (tid == 0) s_nmiss = 0;
+      __syncthreads();
+      for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;  // the staged scores are consumed
+      for (int q0 = warp * 32; q0 < nu; q0 += kThreads) {
+        const int q = q0 + lane;
+        const int sl = q < nu ? int(ulist[q]) : -1;
+        const bool miss = sl >= 0 && !(meta[sl] & kKnown);
+        const unsigned bal = __ballot_sync(0xffffffffu, miss);
+        int base = 0;
+        if (lane == 0 && bal) base = atomicAdd(&s_nmiss, __popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (miss) misslist[base + __popc(bal & ((1u << lane) - 1u))] = int16_t(sl);
+      }
+      __syncthreads();
+      clist = misslist;
+      ncl = s_nmiss;
+    }
+    // ---- C  Hamming once per distinct id without a cached score (groups of 8
+    //         lanes, CB candidates in flight per group)
     {
       const uint4 mine = sub < sk_chunks ? my_sk[sub] : make_uint4(0, 0, 0, 0);
-      for (int wbase = warp * 4; wbase < nu; wbase += CB * kGroups) {
+      for (int wbase = warp * 4; wbase < ncl; wbase += CB * kGroups) {
         const int base = wbase + slot8;
         uint4 v[CB];
         int sl[CB];
 #pragma unroll
         for (int u = 0; u < CB; ++u) {
           const int q = base + u * kGroups;
-          sl[u] = q < nu ? int(ulist[q]) : -1;
+          sl[u] = q < ncl ? int(clist[q]) : -1;
           v[u] = make_uint4(0, 0, 0, 0);
           if (sl[u] >= 0 && sub < sk_chunks) {
             const int32_t id = int32_t(uint32_t(key[sl[u]]) & 0x7fffffffu);
@@ -285,7 +372,8 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     }
     __syncthreads();
     const int cnt = s_cnt;
-    my_cands += unsigned(nu);
+    my_cands += unsigned(ncl);
+    my_distinct += unsigned(nu);
     if (cnt > R) {
       // bins from h = 1024 down: thread t sums bins 4t..4t+3 (index x = 1024 - h);
       // bin x = 1024 (h = 0) is handled last
@@ -369,7 +457,9 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
         const uint32_t m = meta[sl];
         const int h = int((m >> 16) & 0x7ffu);
         const bool sel = ht < 0 || h > ht || (h == ht && int(m & kFirstMask) <= jcut);
-        if (sel && !(uint32_t(key[sl]) & kPoolFlag)) need[atomicAdd(&s_nneed, 1)] = int16_t(sl);
+        // a cached rejection stands: the row's threshold never falls, so a
+        // dot once <= it stays <= it
+        if (sel && !(uint32_t(key[sl]) & kPoolFlag) && !(m & kRej)) need[atomicAdd(&s_nneed, 1)] = int16_t(sl);
       }
     }
     __syncthreads();
@@ -403,12 +493,83 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
           pkey[slot] = (((m >> 16) & 0x7ffu) << 13) | (kFirstMask - (m & kFirstMask));
           pid[slot] = id;
           pdot[slot] = acc;
+        } else if (sub == 0 && sl >= 0 && cached) {
+          meta[sl] |= kRej;
         }
       }
     }
     __syncthreads();
-    // ---- G  rank sort by (h desc, first j asc); keys are distinct
+    // ---- F3  the row's cache for the next iteration: this iteration's distinct
+    //          candidates (the first cache_cap of them) with score and flag
+    if (cached) {
+      const int cc = min(nu, ctl.cache_cap);
+      int32_t* cid = ctl.cache_ids + i * ctl.cache_cap;
+      uint16_t* chr = ctl.cache_hr + i * ctl.cache_cap;
+      for (int q = tid; q < cc; q += kThreads) {
+        const int sl = ulist[q];
+        const uint32_t m = meta[sl];
+        cid[q] = int32_t(uint32_t(key[sl]) & 0x7fffffffu);
+        chr[q] = uint16_t((((m >> 16) & 0x7ffu) << 1) | ((m & kRej) ? 1u : 0u));
+      }
+      if (tid == 0) ctl.cache_cnt[i] = cc;
+      __syncthreads();  // stage G/H lays its arrays over the table
+    }
+    // ---- G/H  insertion of the survivors in visit order (pkey descending;
+    //   keys are distinct).  The new pool goes to new_id/new_sc, laid over the
+    //   hash table, which is dead after F2.
     const int P = s_nprom;
+    int32_t* new_id = reinterpret_cast<int32_t*>(meta);
+    int32_t* new_sc = new_id + kMaxK;
+    if (!serial_insert) {
+      // The pool's last score only rises during the visits, and a rejected
+      // survivor's dot is <= the last score at its visit, so the last score
+      // before visit t is the K-th largest of {starting scores} and {dots of
+      // all survivors visited before t}: survivor t is inserted iff fewer
+      // than K of those values are >= its dot.  The final pool is the best K of
+      // (starting entries, inserted survivors) ordered by score, ties to the
+      // starting entries (in pool order) and then to earlier visits -- the
+      // order the shift-insert loop leaves.  Needs a sorted starting pool
+      // without unscored entries (else serial_insert is set).
+      uint32_t* pflag = reinterpret_cast<uint32_t*>(key);  // bits 0..30: starting scores >= dot; 31: inserted
+      for (int p = tid; p < P; p += kThreads) {
+        const int32_t dp = pdot[p];
+        const uint32_t kp = pkey[p];
+        int lo = 0, hi = K;  // first pool position with a score < dp (scores descend)
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (pool_sc[mid] >= dp) lo = mid + 1;
+          else hi = mid;
+        }
+        int c = lo;
+        for (int q = 0; q < P && c < K; ++q) c += (pkey[q] > kp && pdot[q] >= dp) ? 1 : 0;
+        pflag[p] = uint32_t(lo) | (c < K ? 0x80000000u : 0u);
+      }
+      __syncthreads();
+      for (int k = tid; k < K; k += kThreads) {
+        const int32_t s = pool_sc[k];
+        int rank = k;
+        for (int q = 0; q < P && rank < K; ++q) rank += ((pflag[q] >> 31) && pdot[q] > s) ? 1 : 0;
+        if (rank < K) {
+          new_id[rank] = pool_id[k];
+          new_sc[rank] = s;
+        }
+      }
+      for (int p = tid; p < P; p += kThreads) {
+        const uint32_t f = pflag[p];
+        if (!(f >> 31)) continue;
+        const int32_t dp = pdot[p];
+        const uint32_t kp = pkey[p];
+        int rank = int(f & 0x7fffffffu);
+        for (int q = 0; q < P && rank < K; ++q)
+          rank += ((pflag[q] >> 31) && (pdot[q] > dp || (pdot[q] == dp && pkey[q] > kp))) ? 1 : 0;
+        if (rank < K) {
+          new_id[rank] = pid[p];
+          new_sc[rank] = dp;
+        }
+      }
+    } else {
+    // rank sort by (h desc, first j asc), then the reference's shift-insert
+    // loop in warp 0 with the pool held two entries per lane
     for (int p = tid; p < P; p += kThreads) {
       const uint32_t kp = pkey[p];
       int rank = 0;
@@ -416,7 +577,6 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       order[rank] = uint16_t(p);
     }
     __syncthreads();
-    // ---- H  sequential insertion in warp 0, then write-back
     if (warp == 0) {
       int32_t idA = lane < K ? pool_id[lane] : -1, scA = lane < K ? pool_sc[lane] : kScoreMinI;
       int32_t idB = 32 + lane < K ? pool_id[32 + lane] : -1, scB = 32 + lane < K ? pool_sc[32 + lane] : kScoreMinI;
@@ -447,21 +607,29 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
           }
         }
       }
-      int changed = 0;
       if (lane < K) {
-        const bool ch = idA != pool_id[lane];
-        changed += ch;
-        if (ch || !inplace) {
-          ids_out[i * K + lane] = idA;
-          scores_out[i * K + lane] = scA;
-        }
+        new_id[lane] = idA;
+        new_sc[lane] = scA;
       }
       if (32 + lane < K) {
-        const bool ch = idB != pool_id[32 + lane];
+        new_id[32 + lane] = idB;
+        new_sc[32 + lane] = scB;
+      }
+    }
+    }
+    __syncthreads();
+    // ---- write-back of the positions whose id changed (every position when
+    //      the output is the other buffer) and the update count
+    if (warp == 0) {
+      const unsigned full = 0xffffffffu;
+      int changed = 0;
+      for (int k = lane; k < K; k += 32) {
+        const int32_t nid = new_id[k];
+        const bool ch = nid != pool_id[k];
         changed += ch;
         if (ch || !inplace) {
-          ids_out[i * K + 32 + lane] = idB;
-          scores_out[i * K + 32 + lane] = scB;
+          ids_out[i * K + k] = nid;
+          scores_out[i * K + k] = new_sc[k];
         }
       }
       for (int o = 16; o > 0; o >>= 1) changed += __shfl_xor_sync(full, changed, o);
@@ -481,6 +649,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     atomicAdd(counters + 0, my_updates);
     atomicAdd(counters + 1, my_cands);
     atomicAdd(counters + 2, my_dots);
+    atomicAdd(counters + 3, my_distinct);
     if (ctl.job_upd && run_job >= 0 && run_upd) atomicAdd(ctl.job_upd + run_job, run_upd);
   }
 }

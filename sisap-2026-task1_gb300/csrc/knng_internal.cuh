@@ -114,7 +114,7 @@ cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int 
 // ---- join.cu ----
 // Per-batch NN-Descent control block in device memory.
 struct JoinCtl {
-  unsigned long long* counters;   // [3]: updates, distinct sketch candidates, reranked rows
+  unsigned long long* counters;   // [4]: updates, sketches scored, reranked rows, distinct candidates
   unsigned long long* job_upd;    // [count]: updates of this iteration per job
   int* job_done;                  // [count]: job stopped (its rows pass through)
   float* job_prev;                // [count]: previous iteration's update rate
@@ -122,7 +122,22 @@ struct JoinCtl {
   int* all_done;                  // [1]
   int* final_buf;                 // [1]: buffer index holding every job's final graph
   long long* upd_log;             // [max_iter][count]: updates per iteration per job
+  // Per-row candidate cache (all null: none).  Row i keeps its previous
+  // iteration's distinct two-hop ids with their Hamming scores and whether the
+  // dot is known to be <= the row's pool threshold (which never falls), so the
+  // next iteration gathers sketches and code rows only for new candidates.
+  int32_t* cache_ids;             // [n][cache_cap]
+  uint16_t* cache_hr;             // [n][cache_cap]: score << 1 | rejected
+  int* cache_cnt;                 // [n]: entries held (0 before the first iteration)
+  int cache_cap;
 };
+// Entries per row of the candidate cache (rows with more distinct candidates
+// keep the first ones; the rest are scored again) and its bytes for n rows.
+constexpr int kCacheCap = 1536;
+inline size_t cache_bytes(int64_t n) {
+  return ((size_t(n) * kCacheCap * 4 + 255) & ~size_t(255)) + ((size_t(n) * kCacheCap * 2 + 255) & ~size_t(255)) +
+         size_t(n) * 4;
+}
 cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, int d, int K, int R,
                         const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out,
                         int32_t* scores_out, const int32_t* row_order, unsigned long long* counters,
@@ -131,7 +146,9 @@ cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, 
 // ctas_per_sm: 4 (64 registers per thread) or 3 (up to 85, no spills);
 // cblock: sketch candidates in flight per 8-lane group in the Hamming stage
 // (2, 4 or 8).  Both are chosen by the autotuner.
-// counters[0] += updates, counters[1] += distinct sketch candidates, counters[2] += reranked rows.
+// counters[0] += updates, counters[1] += sketches scored (distinct candidates
+// without a cached score), counters[2] += reranked rows, counters[3] +=
+// distinct candidates.
 // With jt/ctl: rows of stopped jobs are copied through (when out != in) and
 // per-job updates are added to ctl->job_upd; if ctl->all_done is set the launch
 // does nothing.

@@ -39,7 +39,7 @@ class Params(C.Structure):
         ("leaf_size", C.c_int), ("max_iterations", C.c_int), ("early_stop_rate", C.c_float),
         ("rate_diff_tol", C.c_float), ("quant_mode", C.c_int), ("join_mode", C.c_int),
         ("row_order", C.c_int), ("seed", C.c_uint32), ("device", C.c_int), ("autotune", C.c_int),
-        ("use_graph", C.c_int), ("gram_mode", C.c_int), ("init_mode", C.c_int),
+        ("use_graph", C.c_int), ("gram_mode", C.c_int), ("init_mode", C.c_int), ("join_cache", C.c_int),
     ]
 
 
@@ -50,11 +50,11 @@ class Stats(C.Structure):
         ("updates", C.c_int64 * 64), ("forest_levels", C.c_int64), ("leaves", C.c_int64),
         ("device_s", C.c_double), ("join_ms", C.c_double * 64), ("join_candidates", C.c_int64 * 64),
         ("join_dots", C.c_int64 * 64), ("kernel_launches", C.c_int64), ("join_ctas_per_sm", C.c_int),
-        ("join_cblock", C.c_int), ("graph_used", C.c_int),
+        ("join_cblock", C.c_int), ("graph_used", C.c_int), ("join_distinct", C.c_int64 * 64),
     ]
 
     def as_dict(self):
-        arrays = ("updates", "join_ms", "join_candidates", "join_dots")
+        arrays = ("updates", "join_ms", "join_candidates", "join_dots", "join_distinct")
         d = {f: getattr(self, f) for f, _ in self._fields_ if f not in arrays}
         for f in arrays:
             d[f] = list(getattr(self, f)[: self.iterations])

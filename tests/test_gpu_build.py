@@ -117,6 +117,38 @@ def test_build_natural_and_leaf_order_agree(knng_mod):
     np.testing.assert_array_equal(da, db)
 
 
+@pytest.mark.parametrize("n,d,centres", [(30000, 1024, 300), (12000, 384, 60)])
+def test_candidate_cache_changes_nothing(knng_mod, n, d, centres):
+    """Builds with and without the per-row candidate cache give identical
+    graphs and per-iteration update counts; with it, later iterations score
+    far fewer sketches and rerank far fewer rows."""
+    knng = knng_mod
+    x = synth.mixture(n, d, centres, seed=31)
+    with knng.Context(join_cache=1) as a, knng.Context(join_cache=0) as b:
+        sa, sb = knng.Stats(), knng.Stats()
+        ka, da, _ = a.build(x, None, None, sa)
+        kb, db, _ = b.build(x, None, None, sb)
+    np.testing.assert_array_equal(ka, kb)
+    np.testing.assert_array_equal(da.view(np.uint32), db.view(np.uint32))
+    assert sa.iterations == sb.iterations >= 3
+    it = sa.iterations
+    assert list(sa.updates[:it]) == list(sb.updates[:it])
+    assert sa.join_candidates[0] == sb.join_candidates[0]  # empty cache in the first iteration
+    assert sum(sa.join_candidates[2:it]) < 0.5 * sum(sb.join_candidates[2:it])
+    assert sum(sa.join_dots[2:it]) < 0.5 * sum(sb.join_dots[2:it])
+
+
+def test_candidate_cache_with_the_inplace_join(knng_mod):
+    """The in-place join races like the reference's, so its graphs differ from
+    run to run; with the cache its rows are still valid exact-dot lists."""
+    knng = knng_mod
+    x = synth.mixture(20000, 1024, 200, seed=32)
+    with knng.Context(join_mode=knng.JOIN_INPLACE, join_cache=1) as ctx:
+        k, dd, st = ctx.build(x)
+    assert st.iterations >= 2
+    _check_export(x, k, dd)
+
+
 def test_build_rejects_bad_shapes(knng_mod):
     knng = knng_mod
     with knng.Context() as ctx:
