@@ -86,6 +86,7 @@ struct knng_ctx {
   knng_params prm{};
   int device = 0;
   int num_sms = 0;
+  int pageable_access = 0;  // the device reads pageable host memory coherently (NVLink-C2C / ATS)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   cudaEvent_t jev[2] = {};
@@ -232,7 +233,25 @@ int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_devic
     e = launch_quantize(static_cast<const float*>(rows), n, d, c->prm.quant_mode, codes, sketch, c->stream);
     return e ? cuda_fail(c, e, "quantize") : KNNG_OK;
   }
-  // Host rows: stream fixed-size chunks through two staging buffers; the copy
+  // Host rows the device can read itself -- mapped pinned memory, or any
+  // pageable memory when the device accesses it coherently through the host
+  // page tables (Grace + NVLink-C2C) -- are quantised straight from host
+  // memory by one kernel: no staging copies, at the link's read bandwidth.
+  {
+    cudaPointerAttributes at{};
+    const float* direct = nullptr;
+    if (cudaPointerGetAttributes(&at, rows) == cudaSuccess) {
+      if (at.type == cudaMemoryTypeHost && at.devicePointer) direct = static_cast<const float*>(at.devicePointer);
+      else if (at.type == cudaMemoryTypeUnregistered && c->pageable_access) direct = static_cast<const float*>(rows);
+    } else {
+      cudaGetLastError();  // an unknown pointer takes the staging path
+    }
+    if (direct) {
+      e = launch_quantize(direct, n, d, c->prm.quant_mode, codes, sketch, c->stream);
+      return e ? cuda_fail(c, e, "quantize (host rows)") : KNNG_OK;
+    }
+  }
+  // Otherwise stream fixed-size chunks through two staging buffers; the copy
   // of chunk k+1 (copy stream) overlaps the quantisation of chunk k (context
   // stream), ordered by per-buffer events (the reference streams 2.2M-row
   // hyperslabs the same way, src/main.cpp:165-177).
@@ -604,6 +623,7 @@ int knng_create(knng_ctx** out, const knng_params* p) {
   c->device = c->prm.device;
   if ((e = cudaSetDevice(c->device)) ||
       (e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device)) ||
+      (e = cudaDeviceGetAttribute(&c->pageable_access, cudaDevAttrPageableMemoryAccess, c->device)) ||
       (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking))) {
     delete c;
     return KNNG_E_CUDA;

@@ -17,40 +17,50 @@
 // was evicted with a score <= the rising threshold (rejected), and a
 // candidate whose dot is <= the starting pool[K-1].score is always rejected.
 // So the kernel computes dots for the selected candidates not in the starting
-// pool, keeps those above the starting threshold ("promising"), sorts them by
-// (h desc, j asc) and replays the reference's insertion loop over them in one
-// warp, with the pool held two entries per lane.
+// pool and keeps those above the starting threshold ("survivors"), whose
+// insertion in visit order (h desc, j asc) is then resolved by rank counting.
 //
-// Duplicates: only ~25-30 % of the K*K two-hop candidates of a row are
-// distinct ids, so each row first inserts them into a shared-memory hash table
-// (open addressing, keys = ids).  Every occurrence of an id has the same h, so
-// h and the dot are computed once per distinct id.  Among the occurrences of
-// one id only the first in visit order can change the list (a later one finds
-// the id in the list, or scores <= the threshold that evicted or rejected it),
-// and when one occurrence is selected so is the first (ties at the cut are
-// taken in j order), so the visit key of a distinct id is (h, first j).
+// Duplicates: about half of the K*K two-hop candidates of a row repeat an id
+// (1317 distinct of 2500 at 6.35M rows), so each row first inserts them into a
+// shared-memory hash table (open addressing, keys = ids).  Every occurrence of
+// an id has the same h, so h and the dot are computed once per distinct id.
+// Among the occurrences of one id only the first in visit order can change
+// the list (a later one finds the id in the list, or scores <= the threshold
+// that evicted or rejected it), and when one occurrence is selected so is the
+// first (ties at the cut are taken in j order), so the visit key of a
+// distinct id is (h, first j).
 //
-// Stages per row (shared memory, K = 50, R = 400, d = 1024: ~55 KB):
-//   A  own list, sketch, code row; clear table and histogram; insert the
+// Across iterations a row's candidate set barely changes (over 80 % of the
+// distinct ids recur from the third iteration on), and its pool threshold
+// never falls, so with the candidate cache each row keeps its distinct ids
+// with their h and a "dot <= threshold" flag for the next iteration.
+//
+// Stages per row (shared memory, K = 50, R = 400, d = 1024: ~54 KB):
+//   A  own list, sketch, code row; clear table and histogram; start copying
+//      the row's cache entries into shared memory (cp.async); insert the
 //      starting list's ids with a real score, flagged (bit 31 of the key)
 //   B  two-hop ids: warp per neighbour row (K contiguous ids), insert each,
-//      record its slot per j and the first j per slot (atomicMin)
-//   C  Hamming once per distinct id (the first occurrence of an id appends
-//      its slot to the distinct list during B); CB candidates in flight per
-//      8-lane group (the autotuned candidate block):
-//      8 lanes per candidate, one 16-byte sketch chunk per lane (128-byte
-//      rows = one line per candidate), warp __popc
+//      record its slot per j and the first j per slot (atomicMin); the first
+//      occurrence to touch a slot appends it to the distinct list
+//   B2 cached h / rejected flags of the distinct ids; the rest form the miss
+//      list
+//   C  Hamming of the misses, CB in flight per 8-lane group (the autotuned
+//      candidate block): one 16-byte sketch chunk per lane (128-byte rows =
+//      one line per candidate), group __popc
 //   D  histogram of h over all occurrences, threshold h_t (warp scan)
 //   E  selection: every occurrence with h > h_t plus the first
 //      R - count(h > h_t) occurrences with h == h_t in j order; one block scan
 //      of per-thread tie counts finds the cut position, then each distinct id
 //      is selected from its h and first j
-//   F  selected ids not flagged as starting-list members: dp4a dots, 8 lanes
-//      per candidate; keep those above the starting pool[K-1].score
-//   G  rank-sort the survivors by (h desc, first j asc)
-//   H  sequential insertion + write-back + update count (warp 0)
+//   F  selected ids neither flagged as starting-list members nor known to be
+//      rejected: dp4a dots, 8 lanes per candidate; keep those above the
+//      starting pool[K-1].score, flag the others as rejected
+//   F3 write the row's cache: this iteration's distinct ids, h and flags
+//   G/H insertion by rank counting (or the reference's sequential loop for an
+//      unsorted or unscored pool), write-back, update count
 // Per row HBM/L2 bytes: K*8 (own list) + K*K*4 (two-hop ids) + d + d/8 (own
-// row, sketch) + U*d/8 (U distinct candidates) + r*d (r reranked rows).
+// row, sketch) + U*d/8 (U sketches scored) + r*d (r reranked rows) + 12 per
+// distinct id (cache read and write).
 #include "knng_internal.cuh"
 
 #include <algorithm>

@@ -9,10 +9,12 @@
 // Subnormal inputs are read as zero, as the reference's -ffast-math build does.
 // KNNG_QUANT_ROUND clamps to [-127, 127] and rounds half away from zero.
 //
-// Layout: one thread owns 16 consecutive floats of a row (four 16-byte loads,
-// one 16-byte code store); the four threads of a 64-coordinate sketch word sit
-// in adjacent lanes and assemble it with shuffles.  d % 64 == 0 keeps every
-// quad inside one row.  HBM-bound: 4d + d + d/8 bytes per row.
+// Layout: the rows are one stream of float4; every warp load instruction
+// reads 32 consecutive float4 (512 contiguous bytes) and each lane stores the
+// 4-byte code word of its float4, so both the HBM path and host rows read
+// directly over the CPU link stay coalesced.  A sketch word covers 16
+// consecutive float4 of one row (d % 64 == 0) and is built from ballots.
+// Bound by the input stream: 4d + d + d/8 bytes per row.
 #include "knng_internal.cuh"
 
 namespace knng {
@@ -36,39 +38,52 @@ __device__ __forceinline__ int quant1(float v, int mode, unsigned& bit) {
   return q;
 }
 
-__global__ void __launch_bounds__(256) quantize_kernel(const float4* __restrict__ x, int64_t chunks,
-                                                       int mode, uint4* __restrict__ codes,
-                                                       uint64_t* __restrict__ sketch) {
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  // chunks is a multiple of 4 (d % 64 == 0), so every quad of lanes stays active together
-  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c - (threadIdx.x & 31) < chunks;
-       c += stride) {
-    const bool live = c < chunks;
-    unsigned bits = 0;
-    if (live) {
-      float4 v[4];
+// Bit k of the low 16 bits of x moved to bit 4k.
+__device__ __forceinline__ uint64_t spread4(uint32_t x) {
+  uint64_t v = x & 0xffffu;
+  v = (v | (v << 24)) & 0x000000FF000000FFull;
+  v = (v | (v << 12)) & 0x000F000F000F000Full;
+  v = (v | (v << 6)) & 0x0303030303030303ull;
+  v = (v | (v << 3)) & 0x1111111111111111ull;
+  return v;
+}
+
+// A warp covers 128 consecutive float4 per step and each of its load
+// instructions reads 32 consecutive float4 (512 contiguous bytes), which
+// host memory read over the CPU link needs as much as HBM does.  Lane l
+// quantises float4 base + 32u + l (u = 0..3) into one 4-byte code word; the
+// sketch word of 16 consecutive float4 (64 floats, bit j = float j > 0) is
+// assembled from four ballots by the lane that holds its first float4.
+__global__ void __launch_bounds__(256) quantize_kernel(const float4* __restrict__ x, int64_t nf4, int mode,
+                                                       uint32_t* __restrict__ codes, uint64_t* __restrict__ sketch) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t base = warp * 128; base < nf4; base += nwarps * 128) {
+    float4 v[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) v[u] = __ldcs(x + c * 4 + u);
-      unsigned w[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        unsigned b0, b1, b2, b3;
-        int q0 = quant1(v[u].x, mode, b0), q1 = quant1(v[u].y, mode, b1);
-        int q2 = quant1(v[u].z, mode, b2), q3 = quant1(v[u].w, mode, b3);
-        w[u] = (unsigned(q0) & 0xffu) | ((unsigned(q1) & 0xffu) << 8) | ((unsigned(q2) & 0xffu) << 16) |
-               ((unsigned(q3) & 0xffu) << 24);
-        bits |= (b0 | (b1 << 1) | (b2 << 2) | (b3 << 3)) << (4 * u);
-      }
-      codes[c] = make_uint4(w[0], w[1], w[2], w[3]);
+    for (int u = 0; u < 4; ++u) {
+      const int64_t f = base + 32 * u + lane;
+      v[u] = f < nf4 ? __ldcs(x + f) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    // assemble a 64-bit word from 4 adjacent lanes (16 bits each)
-    const unsigned lane = threadIdx.x & 31;
-    unsigned b1 = __shfl_down_sync(0xffffffffu, bits, 1);
-    unsigned b2 = __shfl_down_sync(0xffffffffu, bits, 2);
-    unsigned b3 = __shfl_down_sync(0xffffffffu, bits, 3);
-    if (live && (lane & 3) == 0) {
-      uint64_t word = uint64_t(bits) | (uint64_t(b1) << 16) | (uint64_t(b2) << 32) | (uint64_t(b3) << 48);
-      sketch[c >> 2] = word;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t f = base + 32 * u + lane;
+      unsigned b0, b1, b2, b3;
+      const int q0 = quant1(v[u].x, mode, b0), q1 = quant1(v[u].y, mode, b1);
+      const int q2 = quant1(v[u].z, mode, b2), q3 = quant1(v[u].w, mode, b3);
+      if (f < nf4)
+        codes[f] = (unsigned(q0) & 0xffu) | ((unsigned(q1) & 0xffu) << 8) | ((unsigned(q2) & 0xffu) << 16) |
+                   ((unsigned(q3) & 0xffu) << 24);
+      const unsigned B0 = __ballot_sync(full, b0), B1 = __ballot_sync(full, b1);
+      const unsigned B2 = __ballot_sync(full, b2), B3 = __ballot_sync(full, b3);
+      // nf4 is a multiple of 16, so a 16-lane group is wholly in range or out
+      if ((lane & 15) == 0 && f < nf4) {
+        const int sh = lane;  // 0 or 16
+        sketch[f >> 4] = spread4(B0 >> sh) | (spread4(B1 >> sh) << 1) | (spread4(B2 >> sh) << 2) |
+                         (spread4(B3 >> sh) << 3);
+      }
     }
   }
 }
@@ -78,16 +93,16 @@ __global__ void __launch_bounds__(256) quantize_kernel(const float4* __restrict_
 cudaError_t launch_quantize(const float* x, int64_t n, int d, int quant_mode, int8_t* codes,
                             uint64_t* sketch, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  const int64_t chunks = n * int64_t(d / 16);
+  const int64_t nf4 = n * int64_t(d / 4);  // a multiple of 16: d % 64 == 0
   int dev = 0, sms = 0;
   KNNG_CUDA_TRY(cudaGetDevice(&dev));
   KNNG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  int64_t want = (chunks + 255) / 256;
-  int64_t cap = int64_t(sms) * 8;
-  int blocks = int(want < cap ? want : cap);
+  const int64_t want = (nf4 + 1023) / 1024;  // 8 warps x 128 float4 per block step
+  const int64_t cap = int64_t(sms) * 8;
+  const int blocks = int(want < cap ? want : cap);
   cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
-  quantize_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(x), chunks, quant_mode,
-                                         reinterpret_cast<uint4*>(codes), sketch);
+  quantize_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(x), nf4, quant_mode,
+                                         reinterpret_cast<uint32_t*>(codes), sketch);
   note_launch();
   return cudaGetLastError();
 }
