@@ -411,27 +411,38 @@ def run_gpu(args):
                "d2h_bytes_per_step": n * prm.k_eval * 8}
         del xh
     # ---- roofline of the dominant kernel (NN-Descent join launches)
+    # Algorithmic bytes per row of one iteration of the reference algorithm:
+    # every one of the K*K two-hop candidates reads its id and its sketch,
+    # R = K*rerank candidates are reranked against their d-byte rows (plus a
+    # 4-byte id), and the row's list is read and written (K * 16).
     last = stats[-1]
     it = last.iterations
     join_ms = [last.join_ms[i] for i in range(it)]
     K = prm.k_build
     W8 = d // 8
-    alg_bytes = []
+    R = K * prm.rerank_mult
+    row_alg = K * K * (4 + W8) + R * (d + 4) + K * 16
+    # What the kernel itself moves (its own counters): distinct sketches scored
+    # (deduplicated, candidate cache), reranked rows not known to be rejected,
+    # the candidate cache read and write, lists and the own row.
+    counted = []
     for i in range(it):
-        rows_b = n * (K * 8 + K * K * 4 + d + W8 + K * 8)  # own list, 2-hop ids, own row+sketch, list write
-        # candidate cache: this iteration's distinct candidates written (6 B each, at most 1536 per row),
-        # the previous iteration's read back
+        rows_b = n * (K * 8 + K * K * 4 + d + W8 + K * 8)
         cache_b = 0
         if prm.join_cache:
             wr = min(last.join_distinct[i], 1536 * n)
             cache_b = 6 * (wr + (min(last.join_distinct[i - 1], 1536 * n) if i else 0))
-        alg_bytes.append(rows_b + last.join_candidates[i] * W8 + last.join_dots[i] * d + cache_b)
+        counted.append(rows_b + last.join_candidates[i] * W8 + last.join_dots[i] * d + cache_b)
     peak, peak_kind = load_peaks()
-    achieved = sum(alg_bytes) / (sum(join_ms) * 1e-3) / 1e9 if it else 0.0
+    secs = sum(join_ms) * 1e-3
+    achieved = n * row_alg * it / secs / 1e9 if it else 0.0
+    achieved_counted = sum(counted) / secs / 1e9 if it else 0.0
     roofline = {"kernel": "join_kernel (NN-Descent iteration)", "bound": "hbm", "achieved": achieved,
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "alg_bytes_per_launch": sum(alg_bytes) / max(1, it),
-                "ms_per_launch": sum(join_ms) / max(1, it)}
+                "traffic": None, "alg_bytes_per_launch": n * row_alg, "alg_bytes_per_row": row_alg,
+                "ms_per_launch": sum(join_ms) / max(1, it),
+                "counted_bytes_per_launch": sum(counted) / max(1, it), "counted_achieved": achieved_counted,
+                "counted_frac": achieved_counted / peak}
     if args.traffic_per_launch:
         roofline["traffic"] = args.traffic_per_launch
     elif args.config == "full":
