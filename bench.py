@@ -470,6 +470,8 @@ def run_gpu(args):
                        "join": "jacobi" if prm.join_mode == 0 else "inplace",
                        "leaf_gram": "tcgen05 bf16" if prm.gram_mode == 1 else "dp4a",
                        "candidate_cache": bool(prm.join_cache),
+                       "join_tuned": {"ctas_per_sm": last.join_ctas_per_sm, "cblock": last.join_cblock,
+                                      "cuda_graph": bool(last.graph_used)},
                        "l2": "inputs (n x d float32) far larger than L2; no flush",
                        "parallelism": f"replicas x{ws}"},
             "build_s": last.build_s, "step_s": last.device_s, "iterations": it,
