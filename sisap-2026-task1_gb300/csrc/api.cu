@@ -82,6 +82,13 @@ struct DevBuf {
   }
 };
 
+// (ctas_per_sm, cblock) of the join for its first two iterations, where most
+// candidates are new, and for the later ones, where the candidate cache serves
+// most of them: the two favour different occupancy/in-flight trade-offs.
+struct JoinCfg {
+  std::pair<int, int> early{4, 4}, late{4, 4};
+};
+
 struct knng_ctx {
   knng_params prm{};
   int device = 0;
@@ -99,8 +106,9 @@ struct knng_ctx {
   // join phase captured as a CUDA graph, reused while the launch key matches
   cudaGraphExec_t join_graph = nullptr;
   std::vector<uintptr_t> join_graph_key;
-  // autotuned join configuration per (d, log2 rows): (ctas_per_sm, cblock)
-  std::map<std::pair<int, int>, std::pair<int, int>> tuned;
+  // autotuned join configurations per (d, log2 rows): (ctas_per_sm, cblock) for
+  // the first two iterations and for the later, cache-served ones
+  std::map<std::pair<int, int>, JoinCfg> tuned;
   std::vector<knng_ctx*> subs;  // contexts of the second and later dimension groups of a batch
   std::vector<DevBuf*> buffers() {
     return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs, &cache};
@@ -288,35 +296,52 @@ struct BJob {
 
 // Times the join configurations on the batch's initial graph (output to the
 // spare buffer, which iteration 0 overwrites) and keeps the fastest per
-// (d, log2 rows).  Returns (ctas_per_sm, cblock).
-std::pair<int, int> autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int32_t* const scs[2],
-                                  const int32_t* order, unsigned long long* scratch_counters) {
+// (d, log2 rows).  The early configuration is timed with no candidate cache;
+// with a cache (cache_ctl), one more launch fills every row's cache from the
+// same graph and the configurations are timed again with all candidates
+// cached, which is what the later iterations look like.  The caller clears
+// the cache before the NN-Descent phase.
+JoinCfg autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int32_t* const scs[2],
+                      const int32_t* order, unsigned long long* scratch_counters, const JoinCtl* cache_ctl) {
   const knng_params& p = c->prm;
   const auto key = std::make_pair(d, int(std::log2(double(N))));
   auto it = c->tuned.find(key);
   if (it != c->tuned.end()) return it->second;
-  std::pair<int, int> best{4, 4};
+  JoinCfg best;
   if (!p.autotune || p.join_mode != KNNG_JOIN_JACOBI) return best;
   if (join_prepare_all(p.k_build, p.k_build * p.rerank_mult, d) != cudaSuccess) {
     c->last_error = std::string("join variants: ") + join_variant_error();
     return best;
   }
   const std::pair<int, int> cand[] = {{4, 4}, {4, 8}, {3, 4}, {3, 8}, {4, 2}};
-  float best_ms = 1e30f;
   const int K = p.k_build;
-  for (const auto& cf : cand) {
-    cudaEventRecord(c->jev[0], c->stream);
-    if (launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
-                    ids[1], scs[1], order, scratch_counters, c->num_sms, c->stream, nullptr, nullptr, cf.first,
-                    cf.second) != cudaSuccess)
-      break;
-    cudaEventRecord(c->jev[1], c->stream);
-    cudaEventSynchronize(c->jev[1]);
-    const float ms = elapsed(c->jev[0], c->jev[1]);
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = cf;
+  auto sweep = [&](const JoinCtl* ctl, std::pair<int, int>* out) {
+    float best_ms = 1e30f;
+    for (const auto& cf : cand) {
+      cudaEventRecord(c->jev[0], c->stream);
+      if (launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
+                      ids[1], scs[1], order, scratch_counters, c->num_sms, c->stream, nullptr, ctl, cf.first,
+                      cf.second) != cudaSuccess)
+        return false;
+      cudaEventRecord(c->jev[1], c->stream);
+      cudaEventSynchronize(c->jev[1]);
+      const float ms = elapsed(c->jev[0], c->jev[1]);
+      if (ms < best_ms) {
+        best_ms = ms;
+        *out = cf;
+      }
     }
+    return true;
+  };
+  if (!sweep(nullptr, &best.early)) return best;
+  best.late = best.early;
+  if (cache_ctl) {
+    if (cudaMemsetAsync(cache_ctl->cache_cnt, 0, size_t(N) * 4, c->stream) != cudaSuccess ||
+        launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
+                    ids[1], scs[1], order, scratch_counters, c->num_sms, c->stream, nullptr, cache_ctl,
+                    best.early.first, best.early.second) != cudaSuccess ||
+        !sweep(cache_ctl, &best.late))
+      return best;
   }
   c->tuned[key] = best;
   return best;
@@ -326,7 +351,7 @@ std::pair<int, int> autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const 
 // the per-job stop check; launches after every job has stopped do nothing.
 cudaError_t join_phase(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int32_t* const scs[2],
                        const int32_t* order, const JobTable& jt, const JoinCtl& ctl, unsigned long long* counters,
-                       std::pair<int, int> cfg, bool capture, const char** step) {
+                       const JoinCfg& cfg, bool capture, const char** step) {
   const knng_params& p = c->prm;
   const int K = p.k_build;
   const bool jac = p.join_mode == KNNG_JOIN_JACOBI;
@@ -339,7 +364,7 @@ cudaError_t join_phase(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int
     if (e) return (*step = "iteration start event", e);
     if ((e = launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[cur],
                          scs[cur], ids[nxt], scs[nxt], order, counters + 4 * it, c->num_sms, c->stream, &jt, &ctl,
-                         cfg.first, cfg.second)))
+                         (it < 2 ? cfg.early : cfg.late).first, (it < 2 ? cfg.early : cfg.late).second)))
       return (*step = "join launch", e);
     e = capture ? cudaEventRecordWithFlags(c->itev[2 * it + 1], c->stream, cudaEventRecordExternal)
                 : cudaEventRecord(c->itev[2 * it + 1], c->stream);
@@ -450,21 +475,28 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   }
   // rows in tree-0 leaf order (no forest with the random init: natural order)
   const int32_t* order = (p.row_order == KNNG_ORDER_LEAF && !random_init) ? c->perm.as<int32_t>() : nullptr;
-  const std::pair<int, int> cfg = autotune_join(c, N, d, ids, scs, order, tune_counters);
+  JoinCtl tune_ctl{};  // the candidate cache alone, for the second autotune sweep
+  tune_ctl.cache_ids = ctl.cache_ids;
+  tune_ctl.cache_hr = ctl.cache_hr;
+  tune_ctl.cache_cnt = ctl.cache_cnt;
+  tune_ctl.cache_cap = ctl.cache_cap;
+  const JoinCfg cfg = autotune_join(c, N, d, ids, scs, order, tune_counters, ctl.cache_ids ? &tune_ctl : nullptr);
   cudaEventRecord(c->ev[3], str);
   // every row starts the phase with an empty candidate cache
   if (ctl.cache_cnt && (e = cudaMemsetAsync(ctl.cache_cnt, 0, size_t(N) * 4, str)))
     return cuda_fail(c, e, "candidate cache reset");
   // NN-Descent, captured once per launch key and replayed
   bool graph_used = false;
-  if ((e = join_prepare(K, K * p.rerank_mult, d, cfg.first, cfg.second)))
+  if ((e = join_prepare(K, K * p.rerank_mult, d, cfg.early.first, cfg.early.second)) ||
+      (e = join_prepare(K, K * p.rerank_mult, d, cfg.late.first, cfg.late.second)))
     return cuda_fail(c, e, (std::string("join variant: ") + join_variant_error()).c_str());
   const char* step = "";
   if (p.use_graph) {
     const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->sketch.p), uintptr_t(c->graph.p),
                                         uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(ctl.cache_ids),
                                         uintptr_t(N), uintptr_t(d),
-                                        uintptr_t(J), uintptr_t(o), uintptr_t(cfg.first), uintptr_t(cfg.second),
+                                        uintptr_t(J), uintptr_t(o), uintptr_t(cfg.early.first), uintptr_t(cfg.early.second),
+                                        uintptr_t(cfg.late.first), uintptr_t(cfg.late.second),
                                         uintptr_t(order != nullptr), uintptr_t(p.join_mode), uintptr_t(MI),
                                         uintptr_t(K), uintptr_t(p.rerank_mult)};
     if (!c->join_graph || c->join_graph_key != key) {
@@ -555,8 +587,8 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   }
   S.forest_levels = levels;
   S.leaves = leaves;
-  S.join_ctas_per_sm = cfg.first;
-  S.join_cblock = cfg.second;
+  S.join_ctas_per_sm = cfg.late.first;  // the configuration of the later iterations
+  S.join_cblock = cfg.late.second;
   S.graph_used = graph_used ? 1 : 0;
   S.kernel_launches = launches() - launches0;
   S.total_s = std::chrono::duration<double>(clk::now() - t_start).count();

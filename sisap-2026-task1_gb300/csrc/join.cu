@@ -86,8 +86,7 @@ constexpr uint32_t kRej = 0x40000000u;      // meta bit 30: dot known to be <= t
 struct JoinSmem {
   int K, R, KK, d, W, HT;
   size_t bytes;
-  size_t o_code, o_sk, o_slot, o_key, o_meta, o_hist, o_ulist, o_need, o_pkey, o_pid, o_pdot, o_order, o_pool_id,
-      o_pool_sc, o_miss;
+  size_t o_code, o_sk, o_slot, o_key, o_meta, o_hist, o_ulist, o_surv, o_pool_id, o_pool_sc, o_miss;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -110,11 +109,7 @@ __host__ __device__ inline JoinSmem join_smem(int K, int R, int d) {
   s.o_hist = o;    o = align16(o + size_t(kHBins) * 4);
   s.o_ulist = o;   o = align16(o + size_t(s.KK) * 2);
   const size_t u0 = o;  // stage C's miss list shares this region with stages F-H
-  s.o_need = o;    o = align16(o + size_t(R) * 2);
-  s.o_pkey = o;    o = align16(o + size_t(R) * 4);
-  s.o_pid = o;     o = align16(o + size_t(R) * 4);
-  s.o_pdot = o;    o = align16(o + size_t(R) * 4);
-  s.o_order = o;   o = align16(o + size_t(R) * 2);
+  s.o_surv = o;    o = align16(o + size_t(R) * 16);  // survivors {visit key, dot, id, flags}
   s.o_miss = u0;  // also stages the row's cached ids (kCacheCap * 4 bytes) before stage B2
   if (o < align16(u0 + size_t(s.KK) * 2)) o = align16(u0 + size_t(s.KK) * 2);
   if (o < align16(u0 + size_t(kCacheCap) * 4)) o = align16(u0 + size_t(kCacheCap) * 4);
@@ -191,14 +186,12 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   uint32_t* meta = reinterpret_cast<uint32_t*>(smem + L.o_meta);
   uint32_t* hist = reinterpret_cast<uint32_t*>(smem + L.o_hist);
   int16_t* ulist = reinterpret_cast<int16_t*>(smem + L.o_ulist);
-  int16_t* need = reinterpret_cast<int16_t*>(smem + L.o_need);
+  int16_t* need = cand_slot;  // stage F: the occurrence slots are dead after stage E
   int16_t* misslist = reinterpret_cast<int16_t*>(smem + L.o_miss);  // shares its region with need..order
   const int32_t* stage_id = reinterpret_cast<const int32_t*>(smem + L.o_miss);  // stage A..B2, same region
   const uint16_t* stage_hr = reinterpret_cast<const uint16_t*>(smem + L.o_hist);  // stage A..B2
-  uint32_t* pkey = reinterpret_cast<uint32_t*>(smem + L.o_pkey);
-  int32_t* pid = reinterpret_cast<int32_t*>(smem + L.o_pid);
-  int32_t* pdot = reinterpret_cast<int32_t*>(smem + L.o_pdot);
-  uint16_t* order = reinterpret_cast<uint16_t*>(smem + L.o_order);
+  int4* surv = reinterpret_cast<int4*>(smem + L.o_surv);
+  uint16_t* order = reinterpret_cast<uint16_t*>(cand_slot);  // serial insertion, after stage F
   int32_t* pool_id = reinterpret_cast<int32_t*>(smem + L.o_pool_id);
   int32_t* pool_sc = reinterpret_cast<int32_t*>(smem + L.o_pool_sc);
   __shared__ int s_cnt, s_ht, s_gt, s_jcut, s_nu, s_nneed, s_nprom, s_nmiss, s_ccnt;
@@ -272,29 +265,33 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     // survivor, and an unsorted pool (possible through the stage entry point)
     // breaks the rank formulas of stage G/H: both take the sequential loop.
     const bool serial_insert = __syncthreads_or(irregular) != 0;
-    // ---- B  (warp per neighbour row, all of the warp's rows loaded first; the
-    //         first occurrence to touch a slot appends it to the distinct list)
+    // ---- B  two-hop occurrences j = k*K + k2 spread over the block (thread t
+    //         takes j = t + 256r), all loaded first; the first occurrence to
+    //         touch a slot appends it to the distinct list
     {
-      constexpr int kRowsPerWarp = kMaxK / kWarps;  // 8
-      int32_t v[2 * kRowsPerWarp];
+      constexpr int kRounds = (kMaxK * kMaxK + kThreads - 1) / kThreads;
+      const uint32_t kdiv = ((1u << 20) + uint32_t(K) - 1) / uint32_t(K);  // j / K = (j * kdiv) >> 20 for j < 4096
+      int32_t v[kRounds];
 #pragma unroll
-      for (int t = 0; t < kRowsPerWarp; ++t) {
-        const int k = warp + kWarps * t;
-        const int32_t n1 = k < K ? pool_id[k] : -1;
-        const bool ok = n1 >= 0 && n1 < n;
-        v[2 * t] = (ok && lane < K) ? ids_in[int64_t(n1) * K + lane] : -1;
-        v[2 * t + 1] = (ok && lane + 32 < K) ? ids_in[int64_t(n1) * K + lane + 32] : -1;
+      for (int t = 0; t < kRounds; ++t) {
+        const int j = tid + kThreads * t;
+        int32_t val = -1;
+        if (j < KK) {
+          const int k = int((uint32_t(j) * kdiv) >> 20);
+          const int32_t n1 = pool_id[k];
+          if (n1 >= 0 && n1 < n) val = ids_in[int64_t(n1) * K + (j - k * K)];
+        }
+        v[t] = val;
       }
       int local_cnt = 0;
 #pragma unroll
-      for (int t = 0; t < 2 * kRowsPerWarp; ++t) {
-        const int k = warp + kWarps * (t >> 1);
-        const int k2 = lane + 32 * (t & 1);
+      for (int t = 0; t < kRounds; ++t) {
+        const int j = tid + kThreads * t;
+        if (kThreads * t >= KK) break;  // block-uniform: no occurrence left for any thread
         const int32_t n2 = v[t];
         int sl = -1;
         bool first = false;
-        if (k < K && k2 < K) {
-          const int j = k * K + k2;
+        if (j < KK) {
           if (n2 >= 0 && n2 < n && n2 != i) sl = table_insert(key, mask, n2, 0u);
           cand_slot[j] = int16_t(sl);
           if (sl >= 0) {
@@ -500,9 +497,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
         if (sub == 0 && sl >= 0 && acc > thr0) {
           const uint32_t m = meta[sl];
           const int slot = atomicAdd(&s_nprom, 1);
-          pkey[slot] = (((m >> 16) & 0x7ffu) << 13) | (kFirstMask - (m & kFirstMask));
-          pid[slot] = id;
-          pdot[slot] = acc;
+          surv[slot] = make_int4(int((((m >> 16) & 0x7ffu) << 13) | (kFirstMask - (m & kFirstMask))), acc, id, 0);
         } else if (sub == 0 && sl >= 0 && cached) {
           meta[sl] |= kRej;
         }
@@ -540,10 +535,14 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       // starting entries (in pool order) and then to earlier visits -- the
       // order the shift-insert loop leaves.  Needs a sorted starting pool
       // without unscored entries (else serial_insert is set).
-      uint32_t* pflag = reinterpret_cast<uint32_t*>(key);  // bits 0..30: starting scores >= dot; 31: inserted
+      // A survivor record is {visit key, dot, id, flags}; flags bit 31 =
+      // inserted, bits 0..30 = starting scores >= dot.  Stage G1 reads only
+      // the first two words of the other records, so writing a record's
+      // flags word does not race with it.
       for (int p = tid; p < P; p += kThreads) {
-        const int32_t dp = pdot[p];
-        const uint32_t kp = pkey[p];
+        const int2 me = *reinterpret_cast<const int2*>(surv + p);
+        const uint32_t kp = uint32_t(me.x);
+        const int32_t dp = me.y;
         int lo = 0, hi = K;  // first pool position with a score < dp (scores descend)
         while (lo < hi) {
           const int mid = (lo + hi) >> 1;
@@ -551,39 +550,50 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
           else hi = mid;
         }
         int c = lo;
-        for (int q = 0; q < P && c < K; ++q) c += (pkey[q] > kp && pdot[q] >= dp) ? 1 : 0;
-        pflag[p] = uint32_t(lo) | (c < K ? 0x80000000u : 0u);
+#pragma unroll 4
+        for (int q = 0; q < P; ++q) {
+          const int2 o = *reinterpret_cast<const int2*>(surv + q);
+          c += (uint32_t(o.x) > kp && o.y >= dp) ? 1 : 0;
+        }
+        surv[p].w = int(uint32_t(lo) | (c < K ? 0x80000000u : 0u));
       }
       __syncthreads();
-      for (int k = tid; k < K; k += kThreads) {
-        const int32_t s = pool_sc[k];
-        int rank = k;
-        for (int q = 0; q < P && rank < K; ++q) rank += ((pflag[q] >> 31) && pdot[q] > s) ? 1 : 0;
-        if (rank < K) {
-          new_id[rank] = pool_id[k];
-          new_sc[rank] = s;
-        }
-      }
-      for (int p = tid; p < P; p += kThreads) {
-        const uint32_t f = pflag[p];
-        if (!(f >> 31)) continue;
-        const int32_t dp = pdot[p];
-        const uint32_t kp = pkey[p];
-        int rank = int(f & 0x7fffffffu);
-        for (int q = 0; q < P && rank < K; ++q)
-          rank += ((pflag[q] >> 31) && (pdot[q] > dp || (pdot[q] == dp && pkey[q] > kp))) ? 1 : 0;
-        if (rank < K) {
-          new_id[rank] = pid[p];
-          new_sc[rank] = dp;
+      // one unit per thread: starting entries 0..K-1, then survivors
+      for (int u = tid; u < K + P; u += kThreads) {
+        if (u < K) {
+          const int32_t s = pool_sc[u];
+          int rank = u;
+#pragma unroll 4
+          for (int q = 0; q < P; ++q) {
+            const int4 o = surv[q];
+            rank += (o.w < 0 && o.y > s) ? 1 : 0;
+          }
+          if (rank < K) {
+            new_id[rank] = pool_id[u];
+            new_sc[rank] = s;
+          }
+        } else {
+          const int4 me = surv[u - K];
+          if (me.w >= 0) continue;  // not inserted
+          int rank = me.w & 0x7fffffff;
+#pragma unroll 4
+          for (int q = 0; q < P; ++q) {
+            const int4 o = surv[q];
+            rank += (o.w < 0 && (o.y > me.y || (o.y == me.y && uint32_t(o.x) > uint32_t(me.x)))) ? 1 : 0;
+          }
+          if (rank < K) {
+            new_id[rank] = me.z;
+            new_sc[rank] = me.y;
+          }
         }
       }
     } else {
     // rank sort by (h desc, first j asc), then the reference's shift-insert
     // loop in warp 0 with the pool held two entries per lane
     for (int p = tid; p < P; p += kThreads) {
-      const uint32_t kp = pkey[p];
+      const uint32_t kp = uint32_t(surv[p].x);
       int rank = 0;
-      for (int q = 0; q < P; ++q) rank += pkey[q] > kp ? 1 : 0;
+      for (int q = 0; q < P; ++q) rank += uint32_t(surv[q].x) > kp ? 1 : 0;
       order[rank] = uint16_t(p);
     }
     __syncthreads();
@@ -593,7 +603,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       const unsigned full = 0xffffffffu;
       for (int rr = 0; rr < P; ++rr) {
         const int p = order[rr];
-        const int32_t id = pid[p], dot = pdot[p];
+        const int32_t id = surv[p].z, dot = surv[p].y;
         if (__any_sync(full, idA == id || idB == id)) continue;
         const int32_t last = (K - 1) < 32 ? __shfl_sync(full, scA, K - 1) : __shfl_sync(full, scB, K - 33);
         if (!(dot > last)) continue;
