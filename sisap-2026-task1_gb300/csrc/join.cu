@@ -39,9 +39,10 @@
 //   A  own list, sketch, code row; clear table and histogram; start copying
 //      the row's cache entries into shared memory (cp.async); insert the
 //      starting list's ids with a real score, flagged (bit 31 of the key)
-//   B  two-hop ids: warp per neighbour row (K contiguous ids), insert each,
-//      record its slot per j and the first j per slot (atomicMin); the first
-//      occurrence to touch a slot appends it to the distinct list
+//   B  two-hop occurrences j = k*K + k2 spread over the block (thread t takes
+//      j = t + 256r), insert each, record its slot per j and the first j per
+//      slot (atomicMin); the first occurrence to touch a slot appends it to
+//      the distinct list
 //   B2 cached h / rejected flags of the distinct ids; the rest form the miss
 //      list
 //   C  Hamming of the misses, CB in flight per 8-lane group (the autotuned
@@ -56,8 +57,9 @@
 //      rejected: dp4a dots, 8 lanes per candidate; keep those above the
 //      starting pool[K-1].score, flag the others as rejected
 //   F3 write the row's cache: this iteration's distinct ids, h and flags
-//   G/H insertion by rank counting (or the reference's sequential loop for an
-//      unsorted or unscored pool), write-back, update count
+//   G/H insertion by rank counting over 16-byte survivor records {visit key,
+//      dot, id, flags} (or the reference's sequential loop for an unsorted or
+//      unscored pool), write-back, update count
 // Per row HBM/L2 bytes: K*8 (own list) + K*K*4 (two-hop ids) + d + d/8 (own
 // row, sketch) + U*d/8 (U sketches scored) + r*d (r reranked rows) + 12 per
 // distinct id (cache read and write).
@@ -195,7 +197,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   int32_t* pool_id = reinterpret_cast<int32_t*>(smem + L.o_pool_id);
   int32_t* pool_sc = reinterpret_cast<int32_t*>(smem + L.o_pool_sc);
   __shared__ int s_cnt, s_ht, s_gt, s_jcut, s_nu, s_nneed, s_nprom, s_nmiss, s_ccnt;
-  __shared__ int32_t s_wsum[kWarps];
+  __shared__ int32_t s_wsum[kWarps], s_wsum2[kWarps];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, sub = lane & 7, slot8 = lane >> 3;
   const int KK = L.KK, W = L.W, nchunk = d / 16, sk_chunks = W / 2;
@@ -206,12 +208,21 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   int run_job = -1;                 // per-job update count kept by warp 0 lane 0
   unsigned long long run_upd = 0;
 
+  // job_done only changes between launches, so a CTA reads each job's flag
+  // once; the next row's index is fetched one row ahead
+  int flag_job = -1, flag_done = 0;
+  int64_t next_i = int64_t(blockIdx.x) < n ? (row_order ? int64_t(row_order[blockIdx.x]) : int64_t(blockIdx.x)) : 0;
   for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
-    const int64_t i = row_order ? int64_t(row_order[r]) : r;
+    const int64_t i = next_i;
+    if (r + gridDim.x < n) next_i = row_order ? int64_t(row_order[r + gridDim.x]) : r + gridDim.x;
     int job = 0;
     if (ctl.job_done) {
       job = job_of(jt, i);
-      if (ctl.job_done[job]) {  // stopped job: its rows pass through unchanged
+      if (job != flag_job) {
+        flag_job = job;
+        flag_done = ctl.job_done[job];
+      }
+      if (flag_done) {  // stopped job: its rows pass through unchanged
         if (!inplace)
           for (int k = tid; k < K; k += kThreads) {
             ids_out[i * K + k] = ids_in[i * K + k];
@@ -307,6 +318,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       }
       if (local_cnt) atomicAdd(&s_cnt, local_cnt);
     }
+    if (cached) cp_async_wait_all();  // this thread's staging copies (stage A); the barrier publishes them
     __syncthreads();
     const int nu = s_nu;
     // ---- B2  candidate cache: the row's distinct candidates of the previous
@@ -316,8 +328,6 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     const int16_t* clist = ulist;
     int ncl = nu;
     if (cached) {
-      cp_async_wait_all();  // this thread's staging copies, issued in stage A
-      __syncthreads();
       const int cc = min(s_ccnt, ctl.cache_cap);
       for (int q = tid; q < cc; q += kThreads) {
         const int sl = table_find(key, mask, stage_id[q]);
@@ -439,11 +449,10 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
           const int t = __shfl_up_sync(0xffffffffu, incl, o);
           if (lane >= o) incl += t;
         }
-        __syncthreads();  // s_wsum was read by the threshold step
-        if (lane == 31) s_wsum[warp] = incl;
+        if (lane == 31) s_wsum2[warp] = incl;
         __syncthreads();
         int rank = incl - eq;
-        for (int w = 0; w < warp; ++w) rank += s_wsum[w];
+        for (int w = 0; w < warp; ++w) rank += s_wsum2[w];
         if (rank < need_eq && need_eq <= rank + eq) {
           for (int j = j0; j < j1; ++j) {
             const int sl = cand_slot[j];
@@ -517,13 +526,12 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
         chr[q] = uint16_t((((m >> 16) & 0x7ffu) << 1) | ((m & kRej) ? 1u : 0u));
       }
       if (tid == 0) ctl.cache_cnt[i] = cc;
-      __syncthreads();  // stage G/H lays its arrays over the table
     }
     // ---- G/H  insertion of the survivors in visit order (pkey descending;
     //   keys are distinct).  The new pool goes to new_id/new_sc, laid over the
     //   hash table, which is dead after F2.
     const int P = s_nprom;
-    int32_t* new_id = reinterpret_cast<int32_t*>(meta);
+    int32_t* new_id = reinterpret_cast<int32_t*>(hist);  // dead after stage E; stage F3 may still read the table
     int32_t* new_sc = new_id + kMaxK;
     if (!serial_insert) {
       // The pool's last score only rises during the visits, and a rejected
