@@ -296,7 +296,8 @@ struct BJob {
 
 // Times the join configurations on the batch's initial graph (output to the
 // spare buffer, which iteration 0 overwrites) and keeps the fastest per
-// (d, log2 rows).  The early configuration is timed with no candidate cache;
+// (d, log2 rows), on the first 1/16 of the rows in visit order.  The early
+// configuration is timed with no candidate cache;
 // with a cache (cache_ctl), one more launch fills every row's cache from the
 // same graph and the configurations are timed again with all candidates
 // cached, which is what the later iterations look like.  The caller clears
@@ -315,6 +316,12 @@ JoinCfg autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int3
   }
   const std::pair<int, int> cand[] = {{4, 4}, {4, 8}, {3, 4}, {3, 8}, {4, 2}};
   const int K = p.k_build;
+  // the sweeps process the first 1/16 of the rows (at least 64 per resident CTA),
+  // so tuning costs about one join launch on the first build of a bucket
+  JoinCtl plain{};
+  plain.row_limit = std::min<int64_t>(N, std::max<int64_t>(N / 16, int64_t(c->num_sms) * 4 * 64));
+  JoinCtl cached = cache_ctl ? *cache_ctl : plain;
+  cached.row_limit = plain.row_limit;
   auto sweep = [&](const JoinCtl* ctl, std::pair<int, int>* out) {
     float best_ms = 1e30f;
     for (const auto& cf : cand) {
@@ -333,14 +340,14 @@ JoinCfg autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int3
     }
     return true;
   };
-  if (!sweep(nullptr, &best.early)) return best;
+  if (!sweep(&plain, &best.early)) return best;
   best.late = best.early;
   if (cache_ctl) {
     if (cudaMemsetAsync(cache_ctl->cache_cnt, 0, size_t(N) * 4, c->stream) != cudaSuccess ||
         launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
-                    ids[1], scs[1], order, scratch_counters, c->num_sms, c->stream, nullptr, cache_ctl,
+                    ids[1], scs[1], order, scratch_counters, c->num_sms, c->stream, nullptr, &cached,
                     best.early.first, best.early.second) != cudaSuccess ||
-        !sweep(cache_ctl, &best.late))
+        !sweep(&cached, &best.late))
       return best;
   }
   c->tuned[key] = best;
@@ -437,6 +444,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   ctl.cache_hr = nullptr;
   ctl.cache_cnt = nullptr;
   ctl.cache_cap = 0;
+  ctl.row_limit = 0;  // every row
   if (p.join_cache && MI > 0) {
     if ((e = c->cache.ensure(cache_bytes(N)))) return cuda_fail(c, e, "candidate cache allocation");
     char* cp = c->cache.as<char>();

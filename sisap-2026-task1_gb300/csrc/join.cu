@@ -211,10 +211,11 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   // job_done only changes between launches, so a CTA reads each job's flag
   // once; the next row's index is fetched one row ahead
   int flag_job = -1, flag_done = 0;
-  int64_t next_i = int64_t(blockIdx.x) < n ? (row_order ? int64_t(row_order[blockIdx.x]) : int64_t(blockIdx.x)) : 0;
-  for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
+  const int64_t nrows = (ctl.row_limit > 0 && ctl.row_limit < n) ? ctl.row_limit : n;
+  int64_t next_i = int64_t(blockIdx.x) < nrows ? (row_order ? int64_t(row_order[blockIdx.x]) : int64_t(blockIdx.x)) : 0;
+  for (int64_t r = blockIdx.x; r < nrows; r += gridDim.x) {
     const int64_t i = next_i;
-    if (r + gridDim.x < n) next_i = row_order ? int64_t(row_order[r + gridDim.x]) : r + gridDim.x;
+    if (r + gridDim.x < nrows) next_i = row_order ? int64_t(row_order[r + gridDim.x]) : r + gridDim.x;
     int job = 0;
     if (ctl.job_done) {
       job = job_of(jt, i);

@@ -130,6 +130,7 @@ struct JoinCtl {
   uint16_t* cache_hr;             // [n][cache_cap]: score << 1 | rejected
   int* cache_cnt;                 // [n]: entries held (0 before the first iteration)
   int cache_cap;
+  int64_t row_limit;              // rows processed (the first ones in visit order); 0: all
 };
 // Entries per row of the candidate cache (rows with more distinct candidates
 // keep the first ones; the rest are scored again) and its bytes for n rows.
