@@ -45,7 +45,7 @@ enum { KNNG_QUANT_TRUNC = 0, KNNG_QUANT_ROUND = 1 };
 enum { KNNG_JOIN_JACOBI = 0, KNNG_JOIN_INPLACE = 1 };
 enum { KNNG_ORDER_NATURAL = 0, KNNG_ORDER_LEAF = 1 };
 enum { KNNG_GRAM_DP4A = 0, KNNG_GRAM_TCGEN05 = 1 };
-enum { KNNG_INIT_FOREST = 0, KNNG_INIT_RANDOM = 1 };
+enum { KNNG_INIT_FOREST = 0, KNNG_INIT_RANDOM = 1, KNNG_INIT_BLOCK = 2 };
 
 /* Build parameters.  Defaults (knng_default_params) are the reference's
  * compile-time constants, src/main.cpp:19-29. */
@@ -66,12 +66,19 @@ typedef struct knng_params {
   int autotune;          /* 1: time the join configurations once per (d, size) */
   int use_graph;         /* 1: replay the NN-Descent phase as a CUDA graph */
   int gram_mode;         /* leaf Gram: KNNG_GRAM_DP4A or KNNG_GRAM_TCGEN05 (bf16 tensor cores) */
-  int init_mode;         /* KNNG_INIT_FOREST (src/main.cpp) or KNNG_INIT_RANDOM, the archived
-                            variant archive/nndescent_optimized.cpp:97-118 (needs n > k_build) */
+  int init_mode;         /* KNNG_INIT_FOREST (src/main.cpp); KNNG_INIT_RANDOM, the archived
+                            variant archive/nndescent_optimized.cpp:97-118 (needs n > k_build);
+                            KNNG_INIT_BLOCK, the archived block-partitioned hybrid
+                            archive/nndescent_hybrid.cpp:98-144 (see block_size, bridges) */
   int join_cache;        /* 1: each row keeps its previous iteration's distinct candidates with
                             their Hamming scores and known rejections (n * 9.2 KB of device
                             memory), so later iterations skip most sketch and row gathers;
                             results are identical either way.  0: no cache. */
+  int block_size;        /* KNNG_INIT_BLOCK: rows per block; each job is split into
+                            max(1, round(n / block_size)) equal consecutive blocks (10000:
+                            the archive's 200000 rows / 20 blocks, nndescent_hybrid.cpp:20-21) */
+  int bridges;           /* KNNG_INIT_BLOCK: last entries of each row replaced by random rows
+                            (2, nndescent_hybrid.cpp:22); drawn with xorshift32 from seed + row */
 } knng_params;
 
 /* Per-build timings and convergence record (seconds, device-timed). */

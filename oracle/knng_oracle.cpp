@@ -358,6 +358,60 @@ int oracle_init_random(const int8_t* codes, int64_t n, int d, const oracle_param
   return 0;
 }
 
+// Block-partitioned hybrid init (archive/nndescent_hybrid.cpp:98-144): the
+// rows are split into nb = max(1, round(n / block_size)) consecutive blocks,
+// block q = [q*n/nb, (q+1)*n/nb) (for the archive's 200000 rows and blocks of
+// 10000 these are its 20 blocks); row i keeps the K best rows of its block by
+// exact int8 dot, its last `bridges` entries (positions K-1, K-2, ...) are
+// replaced by random rows other than i with their dots (duplicates allowed, as
+// in the archive), and the list is sorted by score.  The archive draws the
+// bridges from a per-thread std::mt19937 under a dynamic schedule and breaks
+// ties through partial_sort/sort; here the draws are xorshift32 from seed + i
+// (the random fill of src/main.cpp:271-286) and ties go to the lower id, with
+// duplicates kept in place, so the result is reproducible.  Every block must
+// hold K rows besides i.
+int oracle_init_block(const int8_t* codes, int64_t n, int d, const oracle_params* prm, int block_size, int bridges,
+                      int32_t* ids, int32_t* scores) {
+  const int K = prm->k_build;
+  if (block_size < 1 || bridges < 0 || bridges > K) return -1;
+  int64_t nb = (n + block_size / 2) / block_size;
+  if (nb < 1) nb = 1;
+  if (n / nb < K + 1) return -1;  // the smallest block has floor(n / nb) rows
+  set_threads(prm->threads);
+  auto better = [](const Neighbor& a, const Neighbor& b) {
+    return a.score != b.score ? a.score > b.score : a.id < b.id;
+  };
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t q = i * nb / n;
+    while ((q + 1) * n / nb <= i) ++q;
+    while (q * n / nb > i) --q;
+    const int64_t lo = q * n / nb, hi = (q + 1) * n / nb;
+    std::vector<Neighbor> pool;
+    pool.reserve(size_t(hi - lo));
+    for (int64_t j = lo; j < hi; ++j)
+      if (j != i) pool.push_back({int(j), dot_i8(codes + i * d, codes + j * d, d)});
+    std::partial_sort(pool.begin(), pool.begin() + K, pool.end(), better);
+    pool.resize(size_t(K));
+    uint32_t rs = prm->seed + uint32_t(i);
+    for (int k = 0; k < bridges; ++k) {
+      int64_t r = i;
+      for (int budget = 1 << 20; r == i && budget > 0; --budget) {
+        rs = xorshift32(rs);
+        r = int64_t(uint64_t(rs) % uint64_t(n));
+      }
+      if (r == i) r = (i + 1) % n;  // xorshift32 from a zero state (seed + i == 0) stays at 0
+      pool[size_t(K - 1 - k)] = {int(r), dot_i8(codes + i * d, codes + r * d, d)};
+    }
+    std::stable_sort(pool.begin(), pool.end(), better);
+    for (int k = 0; k < K; ++k) {
+      ids[i * K + k] = pool[size_t(k)].id;
+      scores[i * K + k] = pool[size_t(k)].score;
+    }
+  }
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
 // a5: one NN-Descent iteration.  src/main.cpp:324-430.
 // Row i: candidates are G[G[i][k]][k2] for k, k2 < K in that order, minus i,

@@ -67,6 +67,8 @@ def lib():
         L.oracle_init.argtypes = [C.c_void_p, C.c_int64, C.c_int, P(Params), C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p]
         L.oracle_init_random.argtypes = [C.c_void_p, C.c_int64, C.c_int, P(Params), C.c_void_p, C.c_void_p]
+        L.oracle_init_block.argtypes = [C.c_void_p, C.c_int64, C.c_int, P(Params), C.c_int, C.c_int, C.c_void_p,
+                                        C.c_void_p]
         L.oracle_join_iter.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int64, C.c_int, P(Params),
                                        C.c_void_p, C.c_void_p]
         L.oracle_join_iter.restype = C.c_int64
@@ -144,6 +146,18 @@ def init_random(codes, prm=None):
     sc = np.empty((n, prm.k_build), np.int32)
     if lib().oracle_init_random(_ptr(np.ascontiguousarray(codes)), n, d, C.byref(prm), _ptr(ids), _ptr(sc)):
         raise ValueError("oracle_init_random failed")
+    return ids, sc
+
+
+def init_block(codes, prm=None, block_size=10000, bridges=2):
+    """Block-partitioned hybrid init (archive/nndescent_hybrid.cpp:98-144, reproducible draws)."""
+    prm = prm or params()
+    n, d = codes.shape
+    ids = np.empty((n, prm.k_build), np.int32)
+    sc = np.empty((n, prm.k_build), np.int32)
+    if lib().oracle_init_block(_ptr(np.ascontiguousarray(codes)), n, d, C.byref(prm), block_size, bridges,
+                               _ptr(ids), _ptr(sc)):
+        raise ValueError("oracle_init_block failed (every block needs k_build + 1 rows)")
     return ids, sc
 
 

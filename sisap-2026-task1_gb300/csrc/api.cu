@@ -144,7 +144,10 @@ int check_params(knng_ctx* c, const knng_params& p) {
   if (p.join_mode != KNNG_JOIN_JACOBI && p.join_mode != KNNG_JOIN_INPLACE) return set_error(c, KNNG_E_ARGS, "bad join_mode");
   if (p.row_order != KNNG_ORDER_NATURAL && p.row_order != KNNG_ORDER_LEAF) return set_error(c, KNNG_E_ARGS, "bad row_order");
   if (p.gram_mode != KNNG_GRAM_DP4A && p.gram_mode != KNNG_GRAM_TCGEN05) return set_error(c, KNNG_E_ARGS, "bad gram_mode");
-  if (p.init_mode != KNNG_INIT_FOREST && p.init_mode != KNNG_INIT_RANDOM) return set_error(c, KNNG_E_ARGS, "bad init_mode");
+  if (p.init_mode != KNNG_INIT_FOREST && p.init_mode != KNNG_INIT_RANDOM && p.init_mode != KNNG_INIT_BLOCK)
+    return set_error(c, KNNG_E_ARGS, "bad init_mode");
+  if (p.init_mode == KNNG_INIT_BLOCK && (p.block_size < 1 || p.bridges < 0 || p.bridges > p.k_build))
+    return set_error(c, KNNG_E_ARGS, "block init needs block_size >= 1 and bridges in [0, k_build]");
   if (p.join_cache != 0 && p.join_cache != 1) return set_error(c, KNNG_E_ARGS, "join_cache must be 0 or 1");
   return KNNG_OK;
 }
@@ -464,25 +467,34 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     if ((st = quantize_input(c, jobs[b].rows, jobs[b].n, d, jobs[b].on_dev, hoff[b]))) return st;
   cudaEventRecord(c->ev[1], str);
   int64_t levels = 0, leaves = 0;
-  const bool random_init = p.init_mode == KNNG_INIT_RANDOM;
-  if (random_init) {
+  const bool forest_init = p.init_mode == KNNG_INIT_FOREST;
+  if (p.init_mode == KNNG_INIT_RANDOM) {
     for (int b = 0; b < J; ++b)
       if (hn[b] <= K) return set_error(c, KNNG_E_ARGS, "random init needs n > k_build for every job");
+  } else if (p.init_mode == KNNG_INIT_BLOCK) {
+    for (int b = 0; b < J; ++b) {
+      const int64_t nb = std::max<int64_t>(1, (hn[b] + p.block_size / 2) / p.block_size);
+      if (hn[b] / nb < K + 1) return set_error(c, KNNG_E_ARGS, "block init needs k_build + 1 rows in every block");
+    }
   } else if ((st = run_forest(c->codes.as<int8_t>(), N, d, T, p.leaf_size, p.seed, nullptr, 0, c->perm.as<int32_t>(),
                               c->leaf_flag.as<uint8_t>(), s.fb, str, &levels, &c->last_error, jt, split))) {
     return st;
   }
   cudaEventRecord(c->ev[2], str);
-  if (random_init) {
+  if (p.init_mode == KNNG_INIT_RANDOM) {
     if ((e = launch_init_random(c->codes.as<int8_t>(), d, N, K, p.seed, jt, ids[0], scs[0], c->num_sms, str)))
       return cuda_fail(c, e, "random init");
+  } else if (p.init_mode == KNNG_INIT_BLOCK) {
+    if ((e = launch_init_block(c->codes.as<int8_t>(), d, N, K, p.bridges, p.block_size, p.seed, jt, ids[0], scs[0],
+                               c->num_sms, str)))
+      return cuda_fail(c, e, "block init");
   } else if ((st = run_init(c->codes.as<int8_t>(), N, d, T, p.leaf_size, K, p.seed, c->perm.as<int32_t>(),
                             c->leaf_flag.as<uint8_t>(), ids[0], scs[0], s.ib, str, &leaves, &c->last_error, jt,
                             p.gram_mode))) {
     return st;
   }
-  // rows in tree-0 leaf order (no forest with the random init: natural order)
-  const int32_t* order = (p.row_order == KNNG_ORDER_LEAF && !random_init) ? c->perm.as<int32_t>() : nullptr;
+  // rows in tree-0 leaf order (no forest with the random or block init: natural order)
+  const int32_t* order = (p.row_order == KNNG_ORDER_LEAF && forest_init) ? c->perm.as<int32_t>() : nullptr;
   JoinCtl tune_ctl{};  // the candidate cache alone, for the second autotune sweep
   tune_ctl.cache_ids = ctl.cache_ids;
   tune_ctl.cache_hr = ctl.cache_hr;
@@ -627,6 +639,8 @@ void knng_default_params(knng_params* p) {
   p->gram_mode = KNNG_GRAM_TCGEN05;
   p->init_mode = KNNG_INIT_FOREST;
   p->join_cache = 1;
+  p->block_size = 10000;
+  p->bridges = 2;
 }
 
 const char* knng_status_string(int s) {

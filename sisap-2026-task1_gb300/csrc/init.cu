@@ -351,6 +351,112 @@ __global__ void __launch_bounds__(256) init_random_kernel(const int8_t* __restri
   }
 }
 
+// Block-partitioned hybrid init (archive/nndescent_hybrid.cpp:98-144).  A job
+// of n rows is split into nb = max(1, round(n / block_size)) consecutive
+// blocks, block q = [q*n/nb, (q+1)*n/nb); row i keeps the K best rows of its
+// block by exact int8 dot (ties to the lower id), its last `bridges` entries
+// are replaced by random rows other than i with their dots (duplicates
+// allowed, as in the archive), and the list is stably sorted by (score desc,
+// id asc).  Bridges are xorshift32 draws from seed + (job-local) i, where the
+// archive used a per-thread std::mt19937; the oracle restates this exactly.
+// One warp per row: the row's code sits in shared memory, each lane scores
+// one block member per step, and members above the current K-th key are
+// inserted into the warp's list.  The host checks that every block holds
+// K + 1 rows.
+__global__ void __launch_bounds__(256) init_block_kernel(const int8_t* __restrict__ codes, int d, int64_t n_total,
+                                                         int K, int bridges, int block_size, uint32_t seed,
+                                                         JobTable jt, int32_t* __restrict__ ids,
+                                                         int32_t* __restrict__ scores) {
+  __shared__ __align__(16) int8_t row_code[8][kMaxDim];
+  __shared__ uint64_t fin[8][kMaxK];
+  __shared__ int64_t drawn[8][kMaxK];
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t warps = int64_t(gridDim.x) * 8;
+  const int chunks = d / 16;
+  for (int64_t gi = int64_t(blockIdx.x) * 8 + w; gi < n_total; gi += warps) {
+    const int b = job_of(jt, gi);
+    const int64_t base = jt.off[b], n = jt.n[b], i = gi - base;
+    int64_t nb = (n + block_size / 2) / block_size;
+    if (nb < 1) nb = 1;
+    int64_t q = i * nb / n;
+    while ((q + 1) * n / nb <= i) ++q;
+    while (q * n / nb > i) --q;
+    const int64_t lo = q * n / nb, hi = (q + 1) * n / nb;
+    int4* rc = reinterpret_cast<int4*>(row_code[w]);
+    const int4* src = reinterpret_cast<const int4*>(codes + gi * d);
+    for (int u = lane; u < chunks; u += 32) rc[u] = __ldg(src + u);
+    __syncwarp();
+    uint64_t kA = 0, kB = 0, thr = 0;
+    for (int64_t j0 = lo; j0 < hi; j0 += 32) {
+      const int64_t j = j0 + lane;
+      uint64_t key = 0;
+      if (j < hi && j != i) {
+        const int4* cj = reinterpret_cast<const int4*>(codes + (base + j) * d);
+        int acc = 0;
+        for (int u = 0; u < chunks; ++u) {
+          const int4 a = rc[u], v = __ldg(cj + u);
+          acc = __dp4a(a.x, v.x, acc);
+          acc = __dp4a(a.y, v.y, acc);
+          acc = __dp4a(a.z, v.z, acc);
+          acc = __dp4a(a.w, v.w, acc);
+        }
+        key = make_key(acc, int32_t(j));
+      }
+      unsigned m = __ballot_sync(full, key > thr);
+      while (m) {
+        const int s = __ffs(m) - 1;
+        m &= m - 1;
+        const uint64_t ck = __shfl_sync(full, key, s);
+        if (ck > thr) thr = list_insert(kA, kB, ck, K, lane);
+      }
+    }
+    if (lane < K) fin[w][lane] = kA;
+    if (32 + lane < K) fin[w][32 + lane] = kB;
+    if (lane == 0) {
+      uint32_t rs = seed + uint32_t(i);
+      for (int k = 0; k < bridges; ++k) {
+        int64_t r = i;
+        for (int budget = 1 << 20; r == i && budget > 0; --budget) {
+          rs = xorshift32(rs);
+          r = int64_t(uint64_t(rs) % uint64_t(n));
+        }
+        if (r == i) r = (i + 1) % n;  // xorshift32 from a zero state (seed + i == 0) stays at 0
+        drawn[w][k] = r;
+      }
+    }
+    __syncwarp();
+    for (int k = 0; k < bridges; ++k) {
+      const int64_t r = drawn[w][k];
+      const int4* cr = reinterpret_cast<const int4*>(codes + (base + r) * d);
+      int acc = 0;
+      for (int u = lane; u < chunks; u += 32) {
+        const int4 a = rc[u], v = __ldg(cr + u);
+        acc = __dp4a(a.x, v.x, acc);
+        acc = __dp4a(a.y, v.y, acc);
+        acc = __dp4a(a.z, v.z, acc);
+        acc = __dp4a(a.w, v.w, acc);
+      }
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(full, acc, o);
+      if (lane == 0) fin[w][K - 1 - k] = make_key(acc, int32_t(r));
+    }
+    __syncwarp();
+    // stable rank sort, descending (a bridge can repeat an entry: equal keys
+    // keep their position order)
+    for (int e = lane; e < K; e += 32) {
+      const uint64_t me = fin[w][e];
+      int rank = 0;
+      for (int f = 0; f < K; ++f) {
+        const uint64_t o = fin[w][f];
+        rank += (o > me || (o == me && f < e)) ? 1 : 0;
+      }
+      ids[gi * K + rank] = int32_t(base + key_id(me));
+      scores[gi * K + rank] = key_score(me);
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void export_kernel(const int32_t* __restrict__ ids, const int32_t* __restrict__ scores, int64_t n,
                               int K, int k_eval, const int32_t* __restrict__ id_map, int32_t* __restrict__ knns,
                               float* __restrict__ dists, JobTable jt) {
@@ -453,6 +559,16 @@ cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int 
   const int64_t blocks = std::min<int64_t>((n_total + 7) / 8, int64_t(num_sms) * 16);
   cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   init_random_kernel<<<unsigned(blocks), 256, 0, s>>>(codes, d, n_total, K, seed, jt, ids, scores);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_block(const int8_t* codes, int d, int64_t n_total, int K, int bridges, int block_size,
+                              uint32_t seed, const JobTable& jt, int32_t* ids, int32_t* scores, int num_sms,
+                              cudaStream_t s) {
+  const int64_t blocks = std::min<int64_t>((n_total + 7) / 8, int64_t(num_sms) * 16);
+  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
+  init_block_kernel<<<unsigned(blocks), 256, 0, s>>>(codes, d, n_total, K, bridges, block_size, seed, jt, ids, scores);
   note_launch();
   return cudaGetLastError();
 }

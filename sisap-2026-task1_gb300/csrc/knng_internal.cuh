@@ -110,6 +110,11 @@ cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm,
 // Random initial graph (init_mode KNNG_INIT_RANDOM); every job needs n > K.
 cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int K, uint32_t seed, const JobTable& jt,
                                int32_t* ids, int32_t* scores, int num_sms, cudaStream_t s);
+// Block-partitioned hybrid initial graph (init_mode KNNG_INIT_BLOCK); every
+// block of every job needs k_build + 1 rows (checked by the caller).
+cudaError_t launch_init_block(const int8_t* codes, int d, int64_t n_total, int K, int bridges, int block_size,
+                              uint32_t seed, const JobTable& jt, int32_t* ids, int32_t* scores, int num_sms,
+                              cudaStream_t s);
 
 // ---- join.cu ----
 // Per-batch NN-Descent control block in device memory.

@@ -21,7 +21,7 @@ QUANT_TRUNC, QUANT_ROUND = 0, 1
 JOIN_JACOBI, JOIN_INPLACE = 0, 1
 ORDER_NATURAL, ORDER_LEAF = 0, 1
 GRAM_DP4A, GRAM_TCGEN05 = 0, 1
-INIT_FOREST, INIT_RANDOM = 0, 1
+INIT_FOREST, INIT_RANDOM, INIT_BLOCK = 0, 1, 2
 
 STATUS = {0: "ok", -1: "E_ARGS", -2: "E_DIM", -3: "E_OOM", -4: "E_ADMIT", -5: "E_TIMEOUT", -6: "E_CUDA",
           -7: "E_REPLAY", -8: "E_BUSY", -9: "E_NOTFOUND", -10: "E_SCRATCH"}
@@ -40,6 +40,7 @@ class Params(C.Structure):
         ("rate_diff_tol", C.c_float), ("quant_mode", C.c_int), ("join_mode", C.c_int),
         ("row_order", C.c_int), ("seed", C.c_uint32), ("device", C.c_int), ("autotune", C.c_int),
         ("use_graph", C.c_int), ("gram_mode", C.c_int), ("init_mode", C.c_int), ("join_cache", C.c_int),
+        ("block_size", C.c_int), ("bridges", C.c_int),
     ]
 
 

@@ -234,3 +234,67 @@ def test_random_init_matches_oracle(knng_mod, iters):
     assert st.iterations == itr
     np.testing.assert_array_equal(k, kr)
     np.testing.assert_array_equal(dd, dr)
+
+
+def _oracle_block_build(x, max_iter, block_size, bridges, k_build=50):
+    """Block-partitioned hybrid init (archive/nndescent_hybrid.cpp) + the
+    reference's iteration and early stop, oracle double-buffered stable ties."""
+    prm = oracle.params(threads=1, tie_mode=oracle.TIE_STABLE, jacobi=1, k_build=k_build)
+    codes, sk = oracle.quantize(x)
+    ids, sc = oracle.init_block(codes, prm, block_size=block_size, bridges=bridges)
+    n, K = ids.shape
+    prev, it = np.float32(1.0), 0
+    for it in range(max_iter):
+        up = oracle.join_iter(codes, sk, ids, sc, prm)
+        rate = np.float32(up) / np.float32(n * K)
+        if rate < np.float32(0.04) or (it > 0 and (prev - rate) < np.float32(0.01)):
+            it += 1
+            break
+        prev = rate
+    else:
+        it = max_iter
+    k, d = oracle.export(ids, sc)
+    return k, d, it
+
+
+@pytest.mark.parametrize("iters", [0, 30])
+def test_block_init_matches_oracle(knng_mod, iters):
+    knng = knng_mod
+    x = synth.mixture(4000, 768, 40, seed=62)
+    with knng.Context(init_mode=knng.INIT_BLOCK, block_size=700, bridges=2, max_iterations=iters) as ctx:
+        k, dd, st = ctx.build(x)
+    kr, dr, itr = _oracle_block_build(x, iters, 700, 2)
+    assert st.iterations == itr
+    np.testing.assert_array_equal(k, kr)
+    np.testing.assert_array_equal(dd, dr)
+
+
+def test_block_init_archive_shape_and_batches(knng_mod):
+    """The archive's own shape (K = 15, two bridges, equal blocks) at a small
+    size, and a batch of two block-init jobs equal to the jobs alone."""
+    knng = knng_mod
+    x = synth.mixture(6000, 1024, 60, seed=63)
+    y = synth.mixture(2500, 1024, 25, seed=64)
+    kw = dict(init_mode=knng.INIT_BLOCK, block_size=1000, bridges=2, k_build=15, k_eval=15)
+    with knng.Context(**kw) as ctx:
+        kx, dx, sx = ctx.build(x)
+        ky, dy, _ = ctx.build(y)
+        res, _ = ctx.build_batch([x, y])
+    kr, dr, itr = _oracle_block_build(x, 30, 1000, 2, k_build=15)
+    assert sx.iterations == itr
+    np.testing.assert_array_equal(kx, kr)
+    np.testing.assert_array_equal(dx, dr)
+    np.testing.assert_array_equal(res[0][0], kx)
+    np.testing.assert_array_equal(res[1][0], ky)
+    np.testing.assert_array_equal(res[1][1], dy)
+
+
+def test_block_init_rejects_small_blocks(knng_mod):
+    knng = knng_mod
+    x = synth.mixture(1000, 384, 10, seed=65)
+    with knng.Context(init_mode=knng.INIT_BLOCK, block_size=40) as ctx:  # 25 blocks of 40 < k_build + 1
+        with pytest.raises(knng.KnngError) as e:
+            ctx.build(x)
+        assert e.value.status == -1
+    with pytest.raises(knng.KnngError):
+        knng.Context(init_mode=knng.INIT_BLOCK, bridges=51)
