@@ -266,6 +266,19 @@ int knng_init_graph_noalloc(const int8_t* codes_dev, int64_t n, int d, int num_t
                             const uint8_t* leaf_flag_dev, int32_t* ids_dev, int32_t* scores_dev,
                             void* stream);
 
+/* PCA preprocessing, the reference's scripts/data_prep/apply_pca.py:25-33:
+ * rows (n x d float32, host or device memory) are centred, projected onto the
+ * `dims` principal components of their covariance (largest first, each
+ * component's largest-magnitude entry positive, as sklearn's svd_flip), every
+ * projected row is L2-normalised and rounded to float16 (IEEE half bits) into
+ * out_f16 (n x dims, host or device).  variance_kept (may be NULL) receives the
+ * fraction of the variance the components keep.  Uses cuBLAS and cuSOLVER on
+ * `device`; values agree with sklearn's PCA to float32 precision.  Needs
+ * about 4 n (d + dims) bytes of device memory.  Not part of the build path
+ * (src/main.cpp never uses it). */
+int knng_pca(const float* rows, int64_t n, int d, int dims, int device, uint16_t* out_f16,
+             double* variance_kept);
+
 #ifdef __cplusplus
 }
 #endif

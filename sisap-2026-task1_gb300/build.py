@@ -75,7 +75,7 @@ def build(force=False, verbose=False):
                 print(r.stderr, file=sys.stderr)
     objs = [os.path.join(OUT, os.path.basename(s)[:-3] + ".o") for s in sources]
     if force or jobs or _newer(LIB, objs):
-        _run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs)
+        _run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcublas", "-lcusolver"])  # knng_pca
     host_srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
     host_hdrs = glob.glob(os.path.join(HOST, "*.h"))
     if host_srcs and (force or _newer(CLI, host_srcs + host_hdrs + [LIB])):

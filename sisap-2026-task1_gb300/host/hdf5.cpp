@@ -1118,28 +1118,134 @@ std::vector<uint8_t> attribute_v1(const std::string& name, const std::vector<uin
 
 }  // namespace
 
+namespace {
+
+std::vector<uint8_t> type_f16() {
+  Out o;
+  o.u(0x11, 1);
+  o.u(0x20, 1);  // little-endian, implied leading mantissa bit
+  o.u(15, 1);    // sign bit position
+  o.u(0, 1);
+  o.u(2, 4);
+  o.u(0, 2);
+  o.u(16, 2);
+  o.u(10, 1);
+  o.u(5, 1);
+  o.u(0, 1);
+  o.u(10, 1);
+  o.u(15, 4);
+  return o.b;
+}
+
+size_t elem_bytes(int type_class) { return type_class == 2 ? 2 : 4; }
+
+// Local heap data segment of a symbol-table group: "" at offset 0, the link
+// names, then one free block (its "next" field 1 ends the free list).
+struct HeapSeg {
+  Out seg;
+  std::vector<uint64_t> off;
+  uint64_t free_off = 0;
+};
+HeapSeg heap_seg(const std::vector<std::string>& names) {
+  HeapSeg h;
+  h.seg.zeros(8);
+  for (const auto& nm : names) {
+    h.off.push_back(h.seg.size());
+    h.seg.raw(nm.c_str(), nm.size() + 1);
+    h.seg.pad8();
+  }
+  h.free_off = h.seg.size();
+  h.seg.u(1, 8);
+  h.seg.u(64, 8);
+  h.seg.zeros(48);
+  return h;
+}
+
+size_t group_image_bytes(const std::vector<std::string>& names) {
+  return kBtreeBytes + 32 + heap_seg(names).seg.size() + kSnodBytes;
+}
+
+// [B-tree leaf][heap header][heap data][symbol node] of one group at address
+// `at`; entries are (name, object header address), sorted by name.
+void group_image(Out& m, uint64_t at, const std::vector<std::pair<std::string, uint64_t>>& entries, uint64_t* a_bt,
+                 uint64_t* a_heap) {
+  std::vector<std::string> names;
+  for (const auto& e : entries) names.push_back(e.first);
+  const HeapSeg h = heap_seg(names);
+  *a_bt = at;
+  *a_heap = at + kBtreeBytes;
+  const uint64_t a_seg = *a_heap + 32, a_snod = a_seg + h.seg.size();
+  const size_t bt0 = m.size();
+  m.raw("TREE", 4);
+  m.u(0, 1);
+  m.u(0, 1);
+  m.u(1, 2);
+  m.u(kUndef, 8);
+  m.u(kUndef, 8);
+  m.u(0, 8);
+  m.u(a_snod, 8);
+  m.u(entries.empty() ? 0 : h.off.back(), 8);
+  m.zeros(kBtreeBytes - (m.size() - bt0));
+  m.raw("HEAP", 4);
+  m.u(0, 1);
+  m.zeros(3);
+  m.u(h.seg.size(), 8);
+  m.u(h.free_off, 8);
+  m.u(a_seg, 8);
+  m.raw(h.seg.b.data(), h.seg.size());
+  const size_t sn0 = m.size();
+  m.raw("SNOD", 4);
+  m.u(1, 1);
+  m.u(0, 1);
+  m.u(entries.size(), 2);
+  for (size_t i = 0; i < entries.size(); ++i) {
+    m.u(h.off[i], 8);
+    m.u(entries[i].second, 8);
+    m.u(0, 4);
+    m.u(0, 4);
+    m.zeros(16);
+  }
+  m.zeros(kSnodBytes - (m.size() - sn0));
+}
+
+}  // namespace
+
 void write_file(const std::string& path, const std::vector<WriteDataset>& ds_in, const std::vector<WriteAttr>& attrs) {
   std::vector<WriteDataset> ds(ds_in);
   std::sort(ds.begin(), ds.end(), [](const WriteDataset& a, const WriteDataset& b) { return a.name < b.name; });
-  if (ds.size() > size_t(2 * kLeafK)) fail("at most 8 datasets per file are written");
+  // one level of groups: "group/name"
+  std::vector<std::string> groups;
+  std::vector<std::string> leaf(ds.size()), grp(ds.size());
   for (size_t i = 0; i < ds.size(); ++i) {
-    if (ds[i].name.empty() || ds[i].name.find('/') != std::string::npos) fail("bad dataset name '" + ds[i].name + "'");
-    if (i && ds[i].name == ds[i - 1].name) fail("duplicate dataset name " + ds[i].name);
-    if (ds[i].type_class != 0 && ds[i].type_class != 1) fail("datasets are written as int32 or float32");
+    const std::string& nm = ds[i].name;
+    const size_t s = nm.find('/');
+    if (nm.empty() || s == 0 || s + 1 == nm.size() || (s != std::string::npos && nm.find('/', s + 1) != std::string::npos))
+      fail("bad dataset name '" + nm + "' (one optional group level)");
+    if (i && nm == ds[i - 1].name) fail("duplicate dataset name " + nm);
+    if (ds[i].type_class < 0 || ds[i].type_class > 2) fail("datasets are written as int32, float32 or float16");
+    grp[i] = s == std::string::npos ? "" : nm.substr(0, s);
+    leaf[i] = s == std::string::npos ? nm : nm.substr(s + 1);
+    if (!grp[i].empty() && (groups.empty() || groups.back() != grp[i])) groups.push_back(grp[i]);
   }
-  // Local heap data segment: "" at offset 0, then the link names.
-  Out seg;
-  seg.zeros(8);
-  std::vector<uint64_t> name_off;
-  for (const auto& d : ds) {
-    name_off.push_back(seg.size());
-    seg.raw(d.name.c_str(), d.name.size() + 1);
-    seg.pad8();
-  }
-  const uint64_t free_off = seg.size();
-  seg.u(1, 8);  // next free block: none
-  seg.u(64, 8);
-  seg.zeros(48);
+  std::sort(groups.begin(), groups.end());
+  groups.erase(std::unique(groups.begin(), groups.end()), groups.end());
+  for (const auto& g : groups)
+    for (size_t i = 0; i < ds.size(); ++i)
+      if (grp[i].empty() && leaf[i] == g) fail("name " + g + " is both a dataset and a group");
+  // root entries and each group's entries, sorted by name (libhdf5 binary-searches symbol nodes)
+  std::vector<std::string> root_names;
+  for (size_t i = 0; i < ds.size(); ++i)
+    if (grp[i].empty()) root_names.push_back(leaf[i]);
+  for (const auto& g : groups) root_names.push_back(g);
+  std::sort(root_names.begin(), root_names.end());
+  if (root_names.size() > size_t(2 * kLeafK)) fail("at most 8 entries per group are written");
+  std::vector<std::vector<size_t>> members(groups.size());
+  for (size_t i = 0; i < ds.size(); ++i)
+    if (!grp[i].empty())
+      members[size_t(std::lower_bound(groups.begin(), groups.end(), grp[i]) - groups.begin())].push_back(i);
+  for (const auto& mem : members)
+    if (mem.size() > size_t(2 * kLeafK)) fail("at most 8 entries per group are written");
+
   // Global heap objects for the string attributes.
   std::vector<uint32_t> gidx(attrs.size(), 0);
   Out gobj;
@@ -1156,12 +1262,15 @@ void write_file(const std::string& path, const std::vector<WriteDataset>& ds_in,
   }
   const uint64_t gsize = nobj ? std::max<uint64_t>(kGcolMin, (16 + gobj.size() + 16 + 4095) & ~uint64_t(4095)) : 0;
 
-  auto root_header = [&](uint64_t bt, uint64_t heap, uint64_t gcol) {
-    std::vector<std::pair<int, std::vector<uint8_t>>> msgs;
+  auto symtab_msg = [](uint64_t bt, uint64_t heap) {
     Out st;
     st.u(bt, 8);
     st.u(heap, 8);
-    msgs.emplace_back(0x11, st.b);
+    return st.b;
+  };
+  auto root_header = [&](uint64_t bt, uint64_t heap, uint64_t gcol) {
+    std::vector<std::pair<int, std::vector<uint8_t>>> msgs;
+    msgs.emplace_back(0x11, symtab_msg(bt, heap));
     for (size_t i = 0; i < attrs.size(); ++i) {
       Out v;
       if (attrs[i].is_string) {
@@ -1182,34 +1291,59 @@ void write_file(const std::string& path, const std::vector<WriteDataset>& ds_in,
     lay.u(1, 1);
     lay.u(addr, 8);
     lay.u(bytes, 8);
-    return object_header_v1({{0x01, space_v1(d.dims)}, {0x03, d.type_class == 0 ? type_i32() : type_f32()}, {0x08, lay.b}});
+    const std::vector<uint8_t> t = d.type_class == 0 ? type_i32() : d.type_class == 1 ? type_f32() : type_f16();
+    return object_header_v1({{0x01, space_v1(d.dims)}, {0x03, t}, {0x08, lay.b}});
   };
   std::vector<uint64_t> bytes;
   for (const auto& d : ds) {
-    uint64_t n = 4;
+    uint64_t n = elem_bytes(d.type_class);
     for (uint64_t v : d.dims) n *= v;
     bytes.push_back(n);
   }
-  // Addresses: superblock, root header, B-tree, heap, heap data, symbol
-  // node, global heap, dataset headers, raw data.
+  // Addresses: superblock, root header, root group image, each group's header
+  // and image, global heap, dataset headers, raw data.
   const uint64_t a_root = 96;
-  const uint64_t a_bt = a_root + root_header(0, 0, 0).size();
-  const uint64_t a_heap = a_bt + kBtreeBytes;
-  const uint64_t a_seg = a_heap + 32;
-  const uint64_t a_snod = a_seg + seg.size();
-  const uint64_t a_gcol = a_snod + kSnodBytes;
+  const uint64_t a_rimg = a_root + root_header(0, 0, 0).size();
+  uint64_t at = a_rimg + group_image_bytes(root_names);
+  std::vector<uint64_t> a_ghdr(groups.size()), a_gimg(groups.size());
+  const size_t ghdr_bytes = object_header_v1({{0x11, symtab_msg(0, 0)}}).size();
+  for (size_t g = 0; g < groups.size(); ++g) {
+    std::vector<std::string> names;
+    for (size_t i : members[g]) names.push_back(leaf[i]);
+    a_ghdr[g] = at;
+    a_gimg[g] = at + ghdr_bytes;
+    at = a_gimg[g] + group_image_bytes(names);
+  }
+  const uint64_t a_gcol = at;
+  at += gsize;
   std::vector<uint64_t> a_hdr(ds.size()), a_data(ds.size());
-  uint64_t at = a_gcol + gsize;
   for (size_t i = 0; i < ds.size(); ++i) {
     a_hdr[i] = at;
     at += dataset_header(ds[i], 0, 0).size();
   }
+  const uint64_t meta_end = at;
   for (size_t i = 0; i < ds.size(); ++i) {
     at = (at + 7) & ~uint64_t(7);
     a_data[i] = at;
     at += bytes[i];
   }
   const uint64_t eof = at;
+
+  // root entries with their object header addresses
+  std::vector<std::pair<std::string, uint64_t>> root_entries;
+  for (const auto& nm : root_names) {
+    uint64_t a = 0;
+    for (size_t i = 0; i < ds.size(); ++i)
+      if (grp[i].empty() && leaf[i] == nm) a = a_hdr[i];
+    for (size_t g = 0; g < groups.size(); ++g)
+      if (groups[g] == nm) a = a_ghdr[g];
+    root_entries.emplace_back(nm, a);
+  }
+  uint64_t r_bt = 0, r_heap = 0;
+  {
+    Out probe;
+    group_image(probe, a_rimg, root_entries, &r_bt, &r_heap);
+  }
 
   Out m;
   m.raw(kSig, 8);
@@ -1232,42 +1366,23 @@ void write_file(const std::string& path, const std::vector<WriteDataset>& ds_in,
   m.u(a_root, 8);
   m.u(1, 4);  // cache type: symbol table
   m.u(0, 4);
-  m.u(a_bt, 8);
-  m.u(a_heap, 8);
-  const std::vector<uint8_t> rh = root_header(a_bt, a_heap, a_gcol);
+  m.u(r_bt, 8);
+  m.u(r_heap, 8);
+  const std::vector<uint8_t> rh = root_header(r_bt, r_heap, a_gcol);
   m.raw(rh.data(), rh.size());
-  // Group B-tree: one leaf node pointing at the symbol table node.
-  const size_t bt0 = m.size();
-  m.raw("TREE", 4);
-  m.u(0, 1);
-  m.u(0, 1);
-  m.u(1, 2);
-  m.u(kUndef, 8);
-  m.u(kUndef, 8);
-  m.u(0, 8);
-  m.u(a_snod, 8);
-  m.u(ds.empty() ? 0 : name_off.back(), 8);
-  m.zeros(kBtreeBytes - (m.size() - bt0));
-  m.raw("HEAP", 4);
-  m.u(0, 1);
-  m.zeros(3);
-  m.u(seg.size(), 8);
-  m.u(free_off, 8);
-  m.u(a_seg, 8);
-  m.raw(seg.b.data(), seg.size());
-  const size_t sn0 = m.size();
-  m.raw("SNOD", 4);
-  m.u(1, 1);
-  m.u(0, 1);
-  m.u(ds.size(), 2);
-  for (size_t i = 0; i < ds.size(); ++i) {
-    m.u(name_off[i], 8);
-    m.u(a_hdr[i], 8);
-    m.u(0, 4);
-    m.u(0, 4);
-    m.zeros(16);
+  group_image(m, a_rimg, root_entries, &r_bt, &r_heap);
+  for (size_t g = 0; g < groups.size(); ++g) {
+    std::vector<std::pair<std::string, uint64_t>> entries;
+    for (size_t i : members[g]) entries.emplace_back(leaf[i], a_hdr[i]);
+    uint64_t bt = 0, heap = 0;
+    {
+      Out probe;
+      group_image(probe, a_gimg[g], entries, &bt, &heap);
+    }
+    const std::vector<uint8_t> gh = object_header_v1({{0x11, symtab_msg(bt, heap)}});
+    m.raw(gh.data(), gh.size());
+    group_image(m, a_gimg[g], entries, &bt, &heap);
   }
-  m.zeros(kSnodBytes - (m.size() - sn0));
   if (nobj) {
     const size_t g0 = m.size();
     m.raw("GCOL", 4);
@@ -1286,8 +1401,7 @@ void write_file(const std::string& path, const std::vector<WriteDataset>& ds_in,
     const std::vector<uint8_t> h = dataset_header(ds[i], a_data[i], bytes[i]);
     m.raw(h.data(), h.size());
   }
-  if (m.size() != (ds.empty() ? eof : a_hdr.back() + dataset_header(ds.back(), 0, 0).size()))
-    fail("internal layout error while writing " + path);
+  if (m.size() != meta_end) fail("internal layout error while writing " + path);
   File f(path, "wb");
   f.write(m.b.data(), m.size());
   uint64_t pos = m.size();

@@ -12,9 +12,10 @@
 //             shuffle filters (deflate when built with zlib), fixed-point and
 //             IEEE floating-point element types of 1-8 bytes, either byte order;
 //   writing : the layout libhdf5 produces with its default ("earliest")
-//             settings -- superblock v0, a symbol-table root group, v1 object
-//             headers, contiguous datasets, fixed-length string and scalar
-//             float attributes.
+//             settings -- superblock v0, symbol-table groups (the root and one
+//             level below it), v1 object headers, contiguous int32 / float32 /
+//             float16 datasets, variable-length string and scalar float
+//             attributes on the root.
 // Dense (fractal-heap) groups, compound/variable-length element types and
 // other filters are rejected with a clear error.
 #pragma once
@@ -49,8 +50,8 @@ std::vector<int32_t> read_int32(const std::string& path, const std::string& name
 std::vector<std::pair<std::string, std::string>> read_attributes(const std::string& path, const std::string& object);
 
 struct WriteDataset {
-  std::string name;
-  int type_class;  // 0 int32, 1 float32
+  std::string name;  // "name" or "group/name" (one group level)
+  int type_class;    // 0 int32, 1 float32, 2 float16 (raw IEEE half bits)
   std::vector<uint64_t> dims;
   const void* data;
 };

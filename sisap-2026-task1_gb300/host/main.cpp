@@ -18,7 +18,11 @@
 //   knng_main --h5dump FILE [DATASET]   prints the file's datasets and root
 //   attributes (and DATASET's values as float32) as one JSON object;
 //   knng_main --convert SRC DST [--output-format hdf5|knng]   rewrites a
-//   result file (knns, dists, attributes) in the other format.
+//   result file (knns, dists, attributes) in the other format;
+//   knng_main --pca SRC DST DIMS [--device D]   PCA preprocessing on the GPU
+//   (scripts/data_prep/apply_pca.py): /train projected to DIMS components,
+//   L2-normalised, written as float16, with /allknn/knns and /allknn/dists
+//   copied from an HDF5 SRC when present.
 #include <sys/stat.h>
 
 #include <chrono>
@@ -115,8 +119,47 @@ int convert(const std::string& src, const std::string& dst, knngio::Format forma
   }
 }
 
+int pca(const std::string& src, const std::string& dst, int dims, int device) {
+  try {
+    const auto t0 = std::chrono::steady_clock::now();
+    const knngio::Matrix m = knngio::read_matrix(src, "/train");
+    std::cout << "[1] Loaded /train: " << m.rows << " x " << m.cols << "\n";
+    std::vector<uint16_t> out(size_t(m.rows) * size_t(dims));
+    double kept = 0.0;
+    const int st = knng_pca(m.data.data(), m.rows, int(m.cols), dims, device, out.data(), &kept);
+    if (st != KNNG_OK) {
+      std::cerr << "[FATAL] PCA: " << knng_status_string(st) << "\n";
+      return -1;
+    }
+    std::cout << "  -> Variance Retained: " << kept * 100.0 << "%\n";
+    std::vector<knngio::h5::WriteDataset> ds = {{"train", 2, {uint64_t(m.rows), uint64_t(dims)}, out.data()}};
+    std::vector<int32_t> gk;
+    std::vector<float> gd;
+    knngio::h5::DatasetInfo ki, di;
+    if (knngio::h5::is_hdf5(src)) {
+      for (const auto& d : knngio::h5::list_datasets(src)) {
+        if (d.name == "allknn/knns") gk = knngio::h5::read_int32(src, d.name, &ki);
+        if (d.name == "allknn/dists") gd = knngio::h5::read_float(src, d.name, &di);
+      }
+    }
+    if (!gk.empty()) ds.push_back({"allknn/knns", 0, ki.dims, gk.data()});
+    if (!gd.empty()) ds.push_back({"allknn/dists", 1, di.dims, gd.data()});
+    knngio::h5::write_file(dst, ds, {});
+    const std::chrono::duration<double> dt = std::chrono::steady_clock::now() - t0;
+    std::cout << "  -> Saved " << dst << (gk.empty() ? "" : " (with /allknn)") << " in " << dt.count() << " s\n";
+    return 0;
+  } catch (const std::exception& e) {
+    std::cerr << "[FATAL] " << e.what() << "\n";
+    return -1;
+  }
+}
+
 int main(int argc, char** argv) {
   if (argc >= 3 && std::string(argv[1]) == "--h5dump") return h5dump(argv[2], argc >= 4 ? argv[3] : "");
+  if (argc >= 5 && std::string(argv[1]) == "--pca") {
+    const int device = (argc >= 7 && std::string(argv[5]) == "--device") ? std::atoi(argv[6]) : 0;
+    return pca(argv[2], argv[3], std::atoi(argv[4]), device);
+  }
   if (argc >= 4 && std::string(argv[1]) == "--convert") {
     const bool knng = argc >= 6 && std::string(argv[4]) == "--output-format" && std::string(argv[5]) == "knng";
     return convert(argv[2], argv[3], knng ? knngio::Format::kContainer : knngio::Format::kHdf5);

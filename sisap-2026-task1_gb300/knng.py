@@ -65,7 +65,8 @@ class Stats(C.Structure):
 EXPORTS = ["knng_default_params", "knng_create", "knng_destroy", "knng_build", "knng_build_batch", "knng_status_string",
            "knng_last_error", "knng_quantize", "knng_forest", "knng_init_graph", "knng_join_iter", "knng_export",
            "knng_init_graph_noalloc", "knng_footprint_bytes", "knng_trim", "knng_server_default_params",
-           "knng_server_create", "knng_submit", "knng_poll", "knng_wait", "knng_release", "knng_server_destroy"]
+           "knng_server_create", "knng_submit", "knng_poll", "knng_wait", "knng_release", "knng_server_destroy",
+           "knng_pca"]
 
 _lib = None
 
@@ -94,6 +95,7 @@ def lib():
         L.knng_init_graph.argtypes = [V, V, I64, C.c_int, V, V, V, V]
         L.knng_join_iter.argtypes = [V, V, V, I64, C.c_int, V, V, V, V, P(I64)]
         L.knng_export.argtypes = [V, V, I64, C.c_int, C.c_int, V, V, V, V]
+        L.knng_pca.argtypes = [V, I64, C.c_int, C.c_int, C.c_int, V, C.POINTER(C.c_double)]
         L.knng_init_graph_noalloc.argtypes = [V, I64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32, V, V, V, V, V]
         L.knng_footprint_bytes.argtypes = [P(Params), I64, C.c_int, C.c_int]
         L.knng_footprint_bytes.restype = I64
@@ -374,6 +376,21 @@ def quantize(x, quant_mode=QUANT_TRUNC, stream=None):
         raise KnngError(st, "knng_quantize")
     torch.cuda.synchronize(x.device)
     return codes, sk
+
+
+def pca(x, dims, device=0):
+    """PCA preprocessing (scripts/data_prep/apply_pca.py:25-33) on the GPU:
+    returns (float16 (n, dims) L2-normalised projections as numpy, variance kept)."""
+    x = np.ascontiguousarray(np.asarray(x, dtype=np.float32)) if not hasattr(x, "data_ptr") else x
+    n, d = x.shape
+    out = np.empty((n, dims), np.float16)
+    kept = C.c_double(0.0)
+    if hasattr(x, "data_ptr"):
+        _ready(x)
+    st = lib().knng_pca(_ptr(x), n, d, dims, device, out.ctypes.data_as(C.c_void_p), C.byref(kept))
+    if st != 0:
+        raise KnngError(st, "knng_pca")
+    return out, kept.value
 
 
 def export(ids, scores, k_eval=15, id_map=None, stream=None):

@@ -360,12 +360,14 @@ def make_v2(path, rng):
 
 
 def write_datasets(path, arrays, chunks=None, deflate=False):
-    """Write {name: ndarray} (f32/f64/i32/i16/i8/f16, native order) into the
-    root group of a version 0 file: contiguous, or chunked ``chunks`` (one
-    shape for all) over a one-level v1 B-tree, optionally shuffled+deflated."""
+    """Write {name: ndarray} (f32/f64/i32/i16/i8/f16, native order) into a
+    version 0 file, "group/name" into one level of symbol-table groups:
+    contiguous, or chunked ``chunks`` (one shape for all) over a one-level v1
+    B-tree, optionally shuffled+deflated."""
     blob = Blob()
     sb = blob.alloc(96)
     entries = []
+    groups = {}
     for name in sorted(arrays):
         a = np.ascontiguousarray(arrays[name])
         dt = dt_float(a.itemsize) if a.dtype.kind == "f" else dt_int(a.itemsize)
@@ -388,7 +390,16 @@ def write_datasets(path, arrays, chunks=None, deflate=False):
                 pl += struct.pack("<HHHH", 2, 8, 1, 1) + pad8(b"shuffle\0") + struct.pack("<I", a.itemsize) + bytes(4)
                 pl += struct.pack("<HHHH", 1, 8, 0, 1) + pad8(b"deflate\0") + struct.pack("<I", 1) + bytes(4)
                 msgs.insert(2, (0x0B, pl, 0))
-        entries.append((name, blob.add(ohdr_v1(msgs))))
+        hdr = blob.add(ohdr_v1(msgs))
+        if "/" in name:
+            g, leaf = name.split("/", 1)
+            groups.setdefault(g, []).append((leaf, hdr))
+        else:
+            entries.append((name, hdr))
+    for g in sorted(groups):
+        gbt, gheap = symtab_group(blob, sorted(groups[g]))
+        entries.append((g, blob.add(ohdr_v1([(0x11, q(gbt) + q(gheap), 1)]))))
+    entries.sort()
     bt, heap = symtab_group(blob, entries)
     root = blob.add(ohdr_v1([(0x11, q(bt) + q(heap), 1)]))
     blob.put(sb, SIG + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", 4, 16, 0) + q(0) + q(UNDEF) +

@@ -189,3 +189,44 @@ def test_user_block_offset(cli, tmp_path):
     assert np.array_equal(ds["train"], exp)
     got = np.float32(h5dump(cli, tmp_path / "ub.h5", "train")["values"]).reshape(exp.shape)
     assert np.array_equal(got, exp)
+
+
+WRITER_DRIVER = r"""
+#include "hdf5.h"
+#include <cstdint>
+#include <vector>
+int main(int, char** argv) {
+  std::vector<uint16_t> half(6 * 4);
+  for (int i = 0; i < 24; ++i) half[i] = uint16_t(0x3c00 + i);  // 1.0, 1.0009765625, ...
+  std::vector<int32_t> knns(6 * 3);
+  std::vector<float> dists(6 * 3);
+  for (int i = 0; i < 18; ++i) { knns[i] = 7 * i + 1; dists[i] = 0.25f * float(i) - 2.0f; }
+  knngio::h5::write_file(argv[1], {{"train", 2, {6, 4}, half.data()},
+                                   {"allknn/knns", 0, {6, 3}, knns.data()},
+                                   {"allknn/dists", 1, {6, 3}, dists.data()}},
+                         {{"note", true, "groups and halves", 0.0f}});
+  return 0;
+}
+"""
+
+
+def test_writer_groups_and_f16(cli, tmp_path):
+    """The writer's float16 datasets and one group level, read back by both readers."""
+    import hdf5read
+
+    src = tmp_path / "drv.cpp"
+    src.write_text(WRITER_DRIVER)
+    exe = tmp_path / "drv"
+    subprocess.run(["g++", "-std=c++20", "-O1", "-I", os.path.join(PKG, "host"), str(src),
+                    os.path.join(PKG, "host", "hdf5.cpp"), "-o", str(exe)], check=True)
+    subprocess.run([str(exe), str(tmp_path / "g.h5")], check=True)
+    ds, at = hdf5read.read(tmp_path / "g.h5")
+    assert sorted(ds) == ["allknn/dists", "allknn/knns", "train"]
+    want_half = (np.arange(24, dtype=np.uint16) + 0x3C00).view(np.float16).reshape(6, 4)
+    assert ds["train"].dtype == np.float16 and np.array_equal(ds["train"], want_half)
+    assert np.array_equal(ds["allknn/knns"], (7 * np.arange(18) + 1).reshape(6, 3).astype(np.int32))
+    assert np.array_equal(ds["allknn/dists"], (0.25 * np.arange(18) - 2).reshape(6, 3).astype(np.float32))
+    assert at == {"note": "groups and halves"}
+    out = h5dump(cli, tmp_path / "g.h5", "train")
+    assert {d["name"] for d in out["datasets"]} == {"train", "allknn/knns", "allknn/dists"}
+    assert np.array_equal(np.float32(out["values"]).reshape(6, 4), want_half.astype(np.float32))
