@@ -186,7 +186,7 @@ def cpu_port_step(threads, sample=CPU_SAMPLE, seed=4242, want=False):
 
 def recall_parity(x_np, ref_knns, dev):
     """recall@15 (all rows, exact fp64) of the reference port's graph and of the
-    GPU build of the same rows: the benchmark spec's parity measure."""
+    GPU build of the same rows: the parity measure (recall@15 within 0.5 pt)."""
     import torch
 
     import knng
