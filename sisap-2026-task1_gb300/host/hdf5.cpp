@@ -814,6 +814,21 @@ Opened open_dataset(Reader& r, const std::string& name, DatasetInfo* info) {
   if (d.type.cls != 0 && d.type.cls != 1)
     throw std::runtime_error("dataset /" + strip(name) + " has datatype class " + std::to_string(d.type.cls) +
                              " (only integer and floating-point data are read)");
+  // Sizes come from the file: check them before anything is allocated.
+  // Contiguous data must lie inside the file; compressed chunks may expand,
+  // but not past 64 times the file's size.
+  {
+    const uint64_t fsize = r.file().size();
+    long double bytes = d.type.size;
+    for (uint64_t v : d.space.dims) bytes *= (long double)v;
+    const Message* lm = d.obj.find(0x08);
+    if (!lm) throw std::runtime_error("dataset /" + strip(name) + " has no layout message");
+    const Layout l = r.layout(*lm);
+    if (l.cls == 1 && l.addr != kUndef && (long double)r.abs(l.addr) + bytes > (long double)fsize)
+      throw std::runtime_error("dataset /" + strip(name) + " extends past the end of the file");
+    if (bytes > 64.0L * (long double)fsize + 65536.0L)
+      throw std::runtime_error("dataset /" + strip(name) + " is implausibly large for its file");
+  }
   if (info) {
     info->name = strip(name);
     info->type_class = d.type.cls;

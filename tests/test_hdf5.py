@@ -230,3 +230,26 @@ def test_writer_groups_and_f16(cli, tmp_path):
     out = h5dump(cli, tmp_path / "g.h5", "train")
     assert {d["name"] for d in out["datasets"]} == {"train", "allknn/knns", "allknn/dists"}
     assert np.array_equal(np.float32(out["values"]).reshape(6, 4), want_half.astype(np.float32))
+
+
+@pytest.mark.parametrize("fixture", ["h5_v0_chunked.h5", "h5_v2_links.h5"])
+def test_reader_survives_corrupt_files(cli, tmp_path, fixture):
+    """Random byte changes and truncations of a valid file make the reader
+    either succeed or fail with its -1 status and a message, never crash."""
+    import random
+
+    good = open(os.path.join(GOLD, fixture), "rb").read()
+    rng = random.Random(len(good))
+    path = tmp_path / "bad.h5"
+    for trial in range(40):
+        data = bytearray(good)
+        if trial % 5 == 4:
+            data = data[: rng.randrange(8, len(data))]
+        else:
+            for _ in range(rng.randrange(1, 9)):
+                data[rng.randrange(len(data))] = rng.randrange(256)
+        path.write_bytes(bytes(data))
+        for name in (None, "train"):
+            r = subprocess.run([cli, "--h5dump", str(path)] + ([name] if name else []), capture_output=True,
+                               text=True, timeout=30)
+            assert r.returncode in (0, 255), (trial, r.returncode, r.stderr[-200:])
