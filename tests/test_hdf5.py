@@ -253,3 +253,20 @@ def test_reader_survives_corrupt_files(cli, tmp_path, fixture):
             r = subprocess.run([cli, "--h5dump", str(path)] + ([name] if name else []), capture_output=True,
                                text=True, timeout=30)
             assert r.returncode in (0, 255), (trial, r.returncode, r.stderr[-200:])
+
+
+def test_cli_reads_float16_train(cli, tmp_path):
+    """A float16 /train (what the reference's PCA script writes) is read and
+    widened to float32 by the CLI (the build that follows needs a GPU)."""
+    import sys
+
+    sys.path.insert(0, GOLD)
+    import make_hdf5
+
+    x = np.random.default_rng(9).standard_normal((300, 128)).astype(np.float16)
+    make_hdf5.write_datasets(tmp_path / "h.h5", {"train": x}, chunks=(64, 128), deflate=True)
+    out = h5dump(cli, tmp_path / "h.h5", "train")
+    assert out["datasets"][0]["size"] == 2 and out["datasets"][0]["class"] == 1
+    assert np.array_equal(np.float32(out["values"]).reshape(300, 128), x.astype(np.float32))
+    r = subprocess.run([cli, "h.h5"], capture_output=True, text=True, cwd=tmp_path)
+    assert "[OK] Detected 300 vectors in /train." in r.stdout and r.returncode in (0, 255), r.stderr
