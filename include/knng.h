@@ -134,7 +134,11 @@ void knng_destroy(knng_ctx* ctx);
 
 /* Build the all-points kNN graph of n rows of d float32 (row-major).
  * Replaces src/main.cpp:179-457 (quantise, forest, init, NN-Descent, export).
- * rows      : host or device pointer (rows_on_device selects).
+ * rows      : host or device pointer (rows_on_device selects).  Host rows are
+ *             read in place by the quantise kernel when the device can reach
+ *             them (mapped pinned memory, or pageable memory on devices with
+ *             coherent pageable access such as Grace + NVLink-C2C); otherwise
+ *             they are copied through device staging buffers.
  * knns      : n * k_eval int32, 1-based ids, each row worst -> best
  *             (src/main.cpp:452, 455).
  * dists     : n * k_eval float32 int8 inner products, same order (:453, 456).
