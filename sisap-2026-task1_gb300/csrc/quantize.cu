@@ -20,22 +20,23 @@
 namespace knng {
 namespace {
 
-__device__ __forceinline__ int quant1(float v, int mode, unsigned& bit) {
-  if (fabsf(v) < 1.17549435e-38f) v = 0.0f;  // FLT_MIN: subnormals read as zero
-  float s = v * 127.0f;
-  float c;
-  int q;
-  if (mode == KNNG_QUANT_ROUND) {
-    c = (s < 127.0f) ? s : 127.0f;
-    c = (-127.0f < c) ? c : -127.0f;
-    q = __float2int_rz(roundf(c));
-  } else {
-    c = (s < 127.0f) ? s : 127.0f;
-    c = (-128.0f < c) ? c : -128.0f;
-    q = __float2int_rz(c);
-  }
+// x * 127 with subnormal inputs read as zero.  The flush-to-zero multiply
+// gives exactly that for every input: a subnormal x becomes a signed zero, and
+// a normal x has a normal product, so nothing else is flushed.
+__device__ __forceinline__ float scale127_daz(float v) {
+  float s;
+  asm("mul.ftz.f32 %0, %1, %2;" : "=f"(s) : "f"(v), "f"(127.0f));
+  return s;
+}
+
+// The reference's std::max(lo, std::min(127.0f, s)): fminf/fmaxf return the
+// non-NaN operand, so NaN becomes 127 as in std::min(127.0f, NaN).
+template <int kMode>
+__device__ __forceinline__ int quant1(float v, unsigned& bit) {
+  const float s = scale127_daz(v);
+  const float c = fmaxf(fminf(s, 127.0f), kMode == KNNG_QUANT_ROUND ? -127.0f : -128.0f);
   bit = c > 0.0f ? 1u : 0u;
-  return q;
+  return kMode == KNNG_QUANT_ROUND ? __float2int_rz(roundf(c)) : __float2int_rz(c);
 }
 
 // Bit k of the low 16 bits of x moved to bit 4k.
@@ -54,7 +55,8 @@ __device__ __forceinline__ uint64_t spread4(uint32_t x) {
 // quantises float4 base + 32u + l (u = 0..3) into one 4-byte code word; the
 // sketch word of 16 consecutive float4 (64 floats, bit j = float j > 0) is
 // assembled from four ballots by the lane that holds its first float4.
-__global__ void __launch_bounds__(256) quantize_kernel(const float4* __restrict__ x, int64_t nf4, int mode,
+template <int kMode>
+__global__ void __launch_bounds__(256) quantize_kernel(const float4* __restrict__ x, int64_t nf4,
                                                        uint32_t* __restrict__ codes, uint64_t* __restrict__ sketch) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -71,8 +73,8 @@ __global__ void __launch_bounds__(256) quantize_kernel(const float4* __restrict_
     for (int u = 0; u < 4; ++u) {
       const int64_t f = base + 32 * u + lane;
       unsigned b0, b1, b2, b3;
-      const int q0 = quant1(v[u].x, mode, b0), q1 = quant1(v[u].y, mode, b1);
-      const int q2 = quant1(v[u].z, mode, b2), q3 = quant1(v[u].w, mode, b3);
+      const int q0 = quant1<kMode>(v[u].x, b0), q1 = quant1<kMode>(v[u].y, b1);
+      const int q2 = quant1<kMode>(v[u].z, b2), q3 = quant1<kMode>(v[u].w, b3);
       if (f < nf4)
         codes[f] = (unsigned(q0) & 0xffu) | ((unsigned(q1) & 0xffu) << 8) | ((unsigned(q2) & 0xffu) << 16) |
                    ((unsigned(q3) & 0xffu) << 24);
@@ -101,8 +103,10 @@ cudaError_t launch_quantize(const float* x, int64_t n, int d, int quant_mode, in
   const int64_t cap = int64_t(sms) * 8;
   const int blocks = int(want < cap ? want : cap);
   cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
-  quantize_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(x), nf4, quant_mode,
-                                         reinterpret_cast<uint32_t*>(codes), sketch);
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  uint32_t* c4 = reinterpret_cast<uint32_t*>(codes);
+  if (quant_mode == KNNG_QUANT_ROUND) quantize_kernel<KNNG_QUANT_ROUND><<<blocks, 256, 0, s>>>(x4, nf4, c4, sketch);
+  else quantize_kernel<KNNG_QUANT_TRUNC><<<blocks, 256, 0, s>>>(x4, nf4, c4, sketch);
   note_launch();
   return cudaGetLastError();
 }
