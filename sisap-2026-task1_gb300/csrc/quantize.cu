@@ -13,7 +13,7 @@
 // reads 32 consecutive float4 (512 contiguous bytes) and each lane stores the
 // 4-byte code word of its float4, so both the HBM path and host rows read
 // directly over the CPU link stay coalesced.  A sketch word covers 16
-// consecutive float4 of one row (d % 64 == 0) and is built from ballots.
+// consecutive float4 of one row (d % 64 == 0), combined across lanes by shuffles.
 // Bound by the input stream: 4d + d + d/8 bytes per row.
 #include "knng_internal.cuh"
 
@@ -39,22 +39,13 @@ __device__ __forceinline__ int quant1(float v, unsigned& bit) {
   return kMode == KNNG_QUANT_ROUND ? __float2int_rz(roundf(c)) : __float2int_rz(c);
 }
 
-// Bit k of the low 16 bits of x moved to bit 4k.
-__device__ __forceinline__ uint64_t spread4(uint32_t x) {
-  uint64_t v = x & 0xffffu;
-  v = (v | (v << 24)) & 0x000000FF000000FFull;
-  v = (v | (v << 12)) & 0x000F000F000F000Full;
-  v = (v | (v << 6)) & 0x0303030303030303ull;
-  v = (v | (v << 3)) & 0x1111111111111111ull;
-  return v;
-}
-
 // A warp covers 128 consecutive float4 per step and each of its load
 // instructions reads 32 consecutive float4 (512 contiguous bytes), which
 // host memory read over the CPU link needs as much as HBM does.  Lane l
-// quantises float4 base + 32u + l (u = 0..3) into one 4-byte code word; the
-// sketch word of 16 consecutive float4 (64 floats, bit j = float j > 0) is
-// assembled from four ballots by the lane that holds its first float4.
+// quantises float4 base + 32u + l (u = 0..3) into one 4-byte code word and a
+// 4-bit sign nibble; the sketch word of 16 consecutive float4 (64 floats,
+// bit j = float j > 0) takes lane l's nibble at bit 4 (l % 16), combined by
+// three xor-shuffle ORs within 8 lanes and one shuffle for the upper half.
 template <int kMode>
 __global__ void __launch_bounds__(256) quantize_kernel(const float4* __restrict__ x, int64_t nf4,
                                                        uint32_t* __restrict__ codes, uint64_t* __restrict__ sketch) {
@@ -78,14 +69,13 @@ __global__ void __launch_bounds__(256) quantize_kernel(const float4* __restrict_
       if (f < nf4)
         codes[f] = (unsigned(q0) & 0xffu) | ((unsigned(q1) & 0xffu) << 8) | ((unsigned(q2) & 0xffu) << 16) |
                    ((unsigned(q3) & 0xffu) << 24);
-      const unsigned B0 = __ballot_sync(full, b0), B1 = __ballot_sync(full, b1);
-      const unsigned B2 = __ballot_sync(full, b2), B3 = __ballot_sync(full, b3);
+      unsigned w = (b0 | (b1 << 1) | (b2 << 2) | (b3 << 3)) << (4 * (lane & 7));
+      w |= __shfl_xor_sync(full, w, 1);
+      w |= __shfl_xor_sync(full, w, 2);
+      w |= __shfl_xor_sync(full, w, 4);  // lanes 8g..8g+7: their 32 sign bits
+      const unsigned hi = __shfl_down_sync(full, w, 8);
       // nf4 is a multiple of 16, so a 16-lane group is wholly in range or out
-      if ((lane & 15) == 0 && f < nf4) {
-        const int sh = lane;  // 0 or 16
-        sketch[f >> 4] = spread4(B0 >> sh) | (spread4(B1 >> sh) << 1) | (spread4(B2 >> sh) << 2) |
-                         (spread4(B3 >> sh) << 3);
-      }
+      if ((lane & 15) == 0 && f < nf4) sketch[f >> 4] = uint64_t(w) | (uint64_t(hi) << 32);
     }
   }
 }
