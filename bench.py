@@ -247,7 +247,7 @@ def run_reference(args):
     sample = f"{CPU_SAMPLE[0]} x {CPU_SAMPLE[1]} rows, {CPU_SAMPLE[2]} centres, same generator; whole build per step"
     kind, times, walls = "reference", [], []
     for k in range(args.warmup + args.steps):
-        r = cpu_ref_step(threads)
+        r = cpu_ref_step(threads, CPU_SAMPLE)
         if r is None:
             kind = "port"
             break
@@ -257,7 +257,7 @@ def run_reference(args):
     if kind == "port":
         times = []
         for k in range(args.warmup + args.steps):
-            s, _ = cpu_port_step(threads)
+            s, _ = cpu_port_step(threads, CPU_SAMPLE)
             if k >= args.warmup:
                 times.append(s)
         walls = times
