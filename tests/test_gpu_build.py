@@ -1,4 +1,4 @@
-"""Whole builds through knng_build (C ABI), judged as the reference's output is.
+"""Whole builds through knng_build (C ABI), evaluated as the reference's output is.
 
 The graph is nondeterministic in the reference (threads race, nth_element and
 partial_sort ties), so builds are compared by recall@15 against exact float64

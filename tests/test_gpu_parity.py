@@ -3,7 +3,7 @@
 Bit-exact: int8 codes, sign sketches, forest leaf order (replaying the
 reference's own std::mt19937 pivots), initial graph ids and scores, each
 NN-Descent iteration (double-buffered, ties ordered by (hamming desc,
-sequence position asc) in both), export.  Whole builds are judged by
+sequence position asc) in both), export.  Whole builds are evaluated by
 recall@15 against exact float64 brute force, next to the reference binary's
 recall on the same input (tests/golden), within 0.5 points.
 """
