@@ -41,6 +41,12 @@ CONFIGS = {
 CPU_SAMPLE = (100_000, 1024, 1_000)  # bounded CPU sample (the 100k small config), ~10-30 s of CPU work
 METRIC = "vectors/s (kNN-graph build, recall@15-checked)"
 GRAM = {"dp4a": 0, "tc": 1}
+# DRAM read + write bytes per row of one working NN-Descent launch: the mean
+# over the working join launches of one 300k x 1024 build (3k centres), from
+# the one-pass ncu capture summarised in profiles/join_kernel_dram_300k.md.
+JOIN_DRAM_BYTES_PER_ROW_300K = 18962.0
+JOIN_TRAFFIC_SOURCE = ("profiles/join_kernel_dram_300k.md: mean DRAM bytes per row of a 300k build's working "
+                       "join launches (ncu), times this workload's rows")
 
 
 def load_peaks():
@@ -198,19 +204,6 @@ def recall_parity(x_np, ref_knns, dev):
     r_ref = recall_sample(x, torch.from_numpy(ref_knns), rows=x.shape[0])
     r_gpu = recall_sample(x, kg, rows=x.shape[0])
     return {"n": int(x.shape[0]), "reference_port": r_ref, "gpu": r_gpu, "gap_pt": 100 * (r_ref - r_gpu)}
-
-
-def committed_traffic():
-    """DRAM bytes (read + write) per working join launch of the full workload,
-    from the committed ncu summary; None when absent."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "join_kernel_dram_full_6.35M.md")) as f:
-            for ln in f:
-                if ln.startswith("traffic_bytes_per_launch:"):
-                    return float(ln.split(":")[1])
-    except OSError:
-        pass
-    return None
 
 
 def cpu_ref_step(threads, sample=CPU_SAMPLE, seed=4242):
@@ -480,19 +473,28 @@ def run_gpu(args):
         counted.append(rows_b + last.join_candidates[i] * W8 + last.join_dots[i] * d + cache_b)
     peak, peak_kind = load_peaks()
     secs = sum(join_ms) * 1e-3
-    achieved = n * row_alg * it / secs / 1e9 if it else 0.0
+    ms_launch = sum(join_ms) / max(1, it)
+    # DRAM bytes actually moved per launch: the per-row mean of a 300k-row
+    # build's working launches (ncu), times this workload's rows, unless the
+    # caller passes a measured figure for this exact workload.
+    if args.traffic_per_launch:
+        traffic, t_src = args.traffic_per_launch, "--traffic-per-launch"
+    else:
+        traffic, t_src = JOIN_DRAM_BYTES_PER_ROW_300K * n, JOIN_TRAFFIC_SOURCE
+    achieved = traffic / (ms_launch * 1e-3) / 1e9 if it else 0.0
     achieved_counted = sum(counted) / secs / 1e9 if it else 0.0
+    nodedup_rate = n * row_alg * it / secs / 1e9 if it else 0.0
     roofline = {"kernel": "join_kernel (NN-Descent iteration)", "bound": "hbm", "achieved": achieved,
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "alg_bytes_per_launch": n * row_alg, "alg_bytes_per_row": row_alg,
-                "ms_per_launch": sum(join_ms) / max(1, it),
+                "traffic": traffic, "traffic_source": t_src, "ms_per_launch": ms_launch,
                 "counted_bytes_per_launch": sum(counted) / max(1, it), "counted_achieved": achieved_counted,
-                "counted_frac": achieved_counted / peak}
-    if args.traffic_per_launch:
-        roofline["traffic"] = args.traffic_per_launch
-    elif args.config == "full":
-        roofline["traffic"] = committed_traffic()
-        roofline["traffic_source"] = "profiles/join_kernel_dram_full_6.35M.md (ncu, mean of the 7 working launches)"
+                "counted_frac": achieved_counted / peak,
+                "nodedup_bytes_per_launch": n * row_alg, "nodedup_bytes_per_row": row_alg,
+                "nodedup_rate_over_peak": nodedup_rate / peak,
+                "note": "achieved/frac: DRAM bytes moved per launch / launch time; counted_*: the bytes the "
+                        "kernel's own counters say its algorithm must touch (distinct sketches scored, rows "
+                        "reranked, lists, candidate cache); nodedup_*: every two-hop candidate's id and "
+                        "sketch plus R rows per row, an upper bound the kernel avoids by deduplicating"}
     # ---- recall on a seeded sample
     rec = recall_sample(x, knns, rows=args.recall_rows) if args.recall_rows > 0 and rank == 0 else None
     # ---- CPU baseline (rank 0, N=1 only)

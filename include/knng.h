@@ -79,6 +79,16 @@ typedef struct knng_params {
                             the archive's 200000 rows / 20 blocks, nndescent_hybrid.cpp:20-21) */
   int bridges;           /* KNNG_INIT_BLOCK: last entries of each row replaced by random rows
                             (2, nndescent_hybrid.cpp:22); drawn with xorshift32 from seed + row */
+  int wait_limit;        /* polls before a bounded device wait gives up with KNNG_E_TIMEOUT:
+                            0 = the default (2^26); a negative value makes those waits give up
+                            at once (only used to test the timeout path).  The tensor-core leaf
+                            Gram's waits for its tensor-core work; its final drain always keeps
+                            the full limit. */
+  int join_ctas_per_sm;  /* 0: the autotuner picks the NN-Descent kernel variant; 3 or 4 with
+                            join_cblock 2, 4 or 8 forces that variant (resident CTAs per SM x
+                            Hamming candidates in flight) for every iteration and for
+                            knng_join_iter.  Results are identical for every variant. */
+  int join_cblock;
 } knng_params;
 
 /* Per-build timings and convergence record (seconds, device-timed). */

@@ -47,9 +47,13 @@ _lib = None
 
 
 def build():
-    """Compile liboracle.so (and oracle/_ref when the reference sources exist)."""
+    """Compile liboracle.so (and oracle/_ref when the reference sources exist).
+
+    Where the reference sources are is the Makefile's REF variable (settable
+    from the environment); `make have-ref` succeeds only when they are there."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if os.path.isdir("/root/reference/src"):
+    have = subprocess.run(["make", "-s", "-C", HERE, "have-ref"], capture_output=True)
+    if have.returncode == 0:
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 

@@ -149,6 +149,9 @@ int check_params(knng_ctx* c, const knng_params& p) {
   if (p.init_mode == KNNG_INIT_BLOCK && (p.block_size < 1 || p.bridges < 0 || p.bridges > p.k_build))
     return set_error(c, KNNG_E_ARGS, "block init needs block_size >= 1 and bridges in [0, k_build]");
   if (p.join_cache != 0 && p.join_cache != 1) return set_error(c, KNNG_E_ARGS, "join_cache must be 0 or 1");
+  if (p.join_ctas_per_sm != 0 &&
+      (p.join_ctas_per_sm < 3 || p.join_ctas_per_sm > 4 || (p.join_cblock != 2 && p.join_cblock != 4 && p.join_cblock != 8)))
+    return set_error(c, KNNG_E_ARGS, "join_ctas_per_sm must be 0, or 3 or 4 with join_cblock 2, 4 or 8");
   return KNNG_OK;
 }
 
@@ -308,10 +311,14 @@ struct BJob {
 JoinCfg autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int32_t* const scs[2],
                       const int32_t* order, unsigned long long* scratch_counters, const JoinCtl* cache_ctl) {
   const knng_params& p = c->prm;
+  JoinCfg best;
+  if (p.join_ctas_per_sm) {  // a forced variant
+    best.early = best.late = std::make_pair(p.join_ctas_per_sm, p.join_cblock);
+    return best;
+  }
   const auto key = std::make_pair(d, int(std::log2(double(N))));
   auto it = c->tuned.find(key);
   if (it != c->tuned.end()) return it->second;
-  JoinCfg best;
   if (!p.autotune || p.join_mode != KNNG_JOIN_JACOBI) return best;
   if (join_prepare_all(p.k_build, p.k_build * p.rerank_mult, d) != cudaSuccess) {
     c->last_error = std::string("join variants: ") + join_variant_error();
@@ -490,7 +497,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
       return cuda_fail(c, e, "block init");
   } else if ((st = run_init(c->codes.as<int8_t>(), N, d, T, p.leaf_size, K, p.seed, c->perm.as<int32_t>(),
                             c->leaf_flag.as<uint8_t>(), ids[0], scs[0], s.ib, str, &leaves, &c->last_error, jt,
-                            p.gram_mode))) {
+                            p.gram_mode, p.wait_limit))) {
     return st;
   }
   // rows in tree-0 leaf order (no forest with the random or block init: natural order)
@@ -641,6 +648,9 @@ void knng_default_params(knng_params* p) {
   p->join_cache = 1;
   p->block_size = 10000;
   p->bridges = 2;
+  p->wait_limit = 0;
+  p->join_ctas_per_sm = 0;
+  p->join_cblock = 0;
 }
 
 const char* knng_status_string(int s) {
@@ -781,7 +791,8 @@ int knng_init_graph(knng_ctx* c, const int8_t* codes_dev, int64_t n, int d, cons
   JobTable jt;
   if ((st = single_job(c, n, &jt))) return st;
   st = run_init(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.k_build, c->prm.seed, perm_dev,
-                leaf_flag_dev, ids_dev, scores_dev, s.ib, c->stream, nullptr, &c->last_error, jt, c->prm.gram_mode);
+                leaf_flag_dev, ids_dev, scores_dev, s.ib, c->stream, nullptr, &c->last_error, jt, c->prm.gram_mode,
+                c->prm.wait_limit);
   if (st) return st;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   return e ? cuda_fail(c, e, "init") : KNNG_OK;
@@ -800,8 +811,10 @@ int knng_join_iter(knng_ctx* c, const int8_t* codes_dev, const uint64_t* sketch_
   unsigned long long* up = c->scalars.as<unsigned long long>(256);
   if ((e = cudaMemsetAsync(up, 0, 32, c->stream))) return cuda_fail(c, e, "update counter");
   const int K = c->prm.k_build;
+  const int cps = c->prm.join_ctas_per_sm ? c->prm.join_ctas_per_sm : 4;
+  const int cb = c->prm.join_ctas_per_sm ? c->prm.join_cblock : 4;
   if ((e = launch_join(codes_dev, sketch_dev, n, d, K, K * c->prm.rerank_mult, ids_in, scores_in, ids_out,
-                       scores_out, nullptr, up, c->num_sms, c->stream)))
+                       scores_out, nullptr, up, c->num_sms, c->stream, nullptr, nullptr, cps, cb)))
     return cuda_fail(c, e, "join");
   unsigned long long h = 0;
   if ((e = cudaMemcpyAsync(&h, up, 8, cudaMemcpyDeviceToHost, c->stream))) return cuda_fail(c, e, "update count");

@@ -17,9 +17,11 @@
 // to bf16 on the way (TMA cannot convert).  One thread issues 8 MMAs (K = 16
 // each) per stage and commits them to the stage's mbarrier; the stage is
 // refilled only after that barrier flips.  D lives in 128 TMEM columns; warp w
-// reads lanes 32w..32w+31 with tcgen05.ld.  Every mbarrier wait is bounded: on
-// timeout the kernel records kErrTimeout, stops issuing work, waits (bounded)
-// for its committed MMAs and frees its tensor memory before returning.
+// reads lanes 32w..32w+31 with tcgen05.ld.  Every mbarrier wait is bounded (the
+// limit is a launch argument): on timeout the kernel records kErrTimeout, the
+// whole block stops issuing work at the next barrier, thread 0 waits with the
+// full limit for every MMA it committed and the tensor memory is freed before
+// the kernel returns.
 #include "knng_internal.cuh"
 
 #include <algorithm>
@@ -37,8 +39,8 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (long long i = 0; i < kSpinLimit; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit) {
+  for (long long i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
@@ -76,7 +78,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
                                                              const int32_t* __restrict__ perm,
                                                              const int32_t* __restrict__ leaf_start,
                                                              int64_t nleaves, int64_t total,
-                                                             int32_t* __restrict__ gram, unsigned* err) {
+                                                             int32_t* __restrict__ gram, unsigned* err,
+                                                             long long spin_limit) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
@@ -125,15 +128,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
     for (int c = 0; c < nchunks; ++c) {
       const int st = c & 1;
       if (pending[st]) {  // the MMAs that read this stage two chunks ago must be done
-        if (!mbar_wait(smem_u32(&mbar[st]), phase[st])) {
+        if (mbar_wait(smem_u32(&mbar[st]), phase[st], spin_limit)) {
+          phase[st] ^= 1;
+          pending[st] = 0;
+        } else {  // gave up: pending stays set, so the drain below still waits for this commit
           if (tid == 0) atomicOr(err, kErrTimeout);
           s_abort = 1;
         }
-        phase[st] ^= 1;
-        pending[st] = 0;
       }
       __syncthreads();
-      if (s_abort) break;
+      if (s_abort) break;  // block-uniform: s_abort is read after the barrier
       // row tid, 128 codes -> 16 core-matrix rows of 8 bf16 (16 bytes each)
       unsigned char* base = stage[st] + (tid >> 3) * 2048 + (tid & 7) * 16;
 #pragma unroll
@@ -176,13 +180,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
     if (s_abort) break;
     // the last commit covers every MMA of this tile
     const int last = (nchunks - 1) & 1;
-    if (!mbar_wait(smem_u32(&mbar[last]), phase[last])) {
+    if (mbar_wait(smem_u32(&mbar[last]), phase[last], spin_limit)) {
+      phase[last] ^= 1;
+      pending[last] = 0;
+    } else {
       if (tid == 0) atomicOr(err, kErrTimeout);
       s_abort = 1;
-      break;
     }
-    phase[last] ^= 1;
-    pending[last] = 0;
+    __syncthreads();
+    if (s_abort) break;  // block-uniform, as above
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     // warp w reads TMEM lanes 32w..32w+31 = rows of X; warps 0-1 hold leaf 0
     // (columns 0-63), warps 2-3 leaf 1 (columns 64-127)
@@ -208,10 +214,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();  // D is read before the next tile's first MMA overwrites it
   }
-  // drain: wait (bounded) for any commit still outstanding, then free TMEM
+  // drain: wait for any commit still outstanding (thread 0 issued them and
+  // knows which), always with the full limit, so tensor memory is never freed
+  // under an MMA in flight; then free it
   if (tid == 0)
     for (int st = 0; st < 2; ++st)
-      if (pending[st]) mbar_wait(smem_u32(&mbar[st]), phase[st]);
+      if (pending[st]) mbar_wait(smem_u32(&mbar[st]), phase[st], kSpinLimit);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -223,7 +231,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
 
 cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm, const int32_t* leaf_start,
                                 int64_t nleaves, int64_t total, int32_t* gram, unsigned* err, int num_sms,
-                                cudaStream_t s) {
+                                cudaStream_t s, int wait_limit) {
   if (d % kChunk != 0) return cudaErrorInvalidValue;
   const size_t smem = 2 * size_t(kStageBytes) + 1024;
   KNNG_CUDA_TRY(ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram_tc), smem));
@@ -232,7 +240,11 @@ cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm,
   const int64_t blocks = std::min<int64_t>(pairs, int64_t(num_sms) * 2);
   if (blocks <= 0) return cudaSuccess;
   cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
-  leaf_gram_tc<<<unsigned(blocks), kTcThreads, smem, s>>>(codes, d, perm, leaf_start, nleaves, total, gram, err);
+  // wait_limit > 0: polls per wait; 0: the default; < 0: every wait in the
+  // main loop gives up at once (the drain keeps the full limit)
+  const long long spins = wait_limit > 0 ? (long long)wait_limit : wait_limit < 0 ? 0ll : kSpinLimit;
+  leaf_gram_tc<<<unsigned(blocks), kTcThreads, smem, s>>>(codes, d, perm, leaf_start, nleaves, total, gram, err,
+                                                          spins);
   note_launch();
   return cudaGetLastError();
 }

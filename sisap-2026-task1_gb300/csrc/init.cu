@@ -489,7 +489,7 @@ size_t init_bytes(int64_t n, int T, int leaf) {
 
 int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint32_t seed, const int32_t* perm,
              const uint8_t* leaf_flag, int32_t* ids, int32_t* scores, const InitBufs& ib, cudaStream_t s,
-             int64_t* leaves_out, std::string* err, const JobTable& jt, int gram_mode) {
+             int64_t* leaves_out, std::string* err, const JobTable& jt, int gram_mode, int wait_limit) {
   (void)leaf;
   auto fail = [&](cudaError_t e, const char* what) {
     if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
@@ -520,7 +520,7 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
   unsigned* gerr = reinterpret_cast<unsigned*>(ib.dev_i64 + 3);
   if (gram_mode == 1) {
     if ((e = cudaMemsetAsync(gerr, 0, sizeof(unsigned), s))) return fail(e, "gram flag");
-    if ((e = launch_leaf_gram_tc(codes, d, perm, leaf_start, nleaves, tn, ib.gram, gerr, sms, s)))
+    if ((e = launch_leaf_gram_tc(codes, d, perm, leaf_start, nleaves, tn, ib.gram, gerr, sms, s, wait_limit)))
       return fail(e, "tensor-core gram");
   } else {
     const size_t smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;

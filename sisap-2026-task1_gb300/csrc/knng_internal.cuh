@@ -101,11 +101,12 @@ size_t init_bytes(int64_t n, int T, int leaf);
 int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint32_t seed,
              const int32_t* perm, const uint8_t* leaf_flag, int32_t* ids, int32_t* scores,
              const InitBufs& ib, cudaStream_t s, int64_t* leaves_out, std::string* err,
-             const JobTable& jt, int gram_mode = 0);
+             const JobTable& jt, int gram_mode = 0, int wait_limit = 0);
 // gram_mode 0: dp4a leaf Gram (leaf_gram); 1: tcgen05 bf16 tensor-core Gram (leaf_gram_tc)
+// wait_limit: knng_params::wait_limit (0 = default polls per bounded wait)
 cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm, const int32_t* leaf_start,
                                 int64_t nleaves, int64_t total, int32_t* gram, unsigned* err, int num_sms,
-                                cudaStream_t s);
+                                cudaStream_t s, int wait_limit = 0);
 
 // Random initial graph (init_mode KNNG_INIT_RANDOM); every job needs n > K.
 cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int K, uint32_t seed, const JobTable& jt,

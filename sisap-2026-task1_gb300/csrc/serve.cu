@@ -5,9 +5,10 @@
 // No counterpart in the reference, which builds one graph per process
 // (src/main.cpp:114-498).  A server owns `slots` worker threads, each with its
 // own knng_ctx (CUDA stream + stream-ordered buffers).  Submitted jobs wait in
-// one FIFO.  A worker that becomes free takes, from the front of the queue,
-// every job whose footprint (knng_footprint_bytes) still fits in the memory
-// budget next to the batches already running, and builds them as one batch
+// one FIFO.  A worker that becomes free takes, in queue order, every job whose
+// footprint (knng_footprint_bytes) still fits in the memory budget next to the
+// batches already running -- a job that does not fit yet is passed over by
+// later ones at most kMaxBypass times -- and builds them as one batch
 // (knng_build_batch); jobs that arrive while other batches run are therefore
 // admitted as soon as a slot and memory free up, and the batches of different
 // slots run concurrently on their own streams.  A job larger than the whole
@@ -17,6 +18,7 @@
 // of that job alone, whatever it was batched with.
 #include "knng_internal.cuh"
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -36,7 +38,12 @@ struct Ticket {
   bool done = false;
   int status = KNNG_E_BUSY;
   int batch_jobs = 0;
+  int bypassed = 0;  // batches admitted ahead of this job while it did not fit
 };
+
+// How often a queued job that does not fit may be passed over by later,
+// smaller jobs before admission waits for it (no starvation of large jobs).
+constexpr int kMaxBypass = 4;
 
 }  // namespace
 
@@ -67,21 +74,43 @@ void worker_loop(knng_server* sv, int slot) {
       std::unique_lock<std::mutex> lk(sv->mu);
       for (;;) {
         if (sv->stop) return;
-        // refuse jobs that could never fit
-        while (!sv->queue.empty() && sv->tickets[sv->queue.front()].footprint > budget) {
-          Ticket& t = sv->tickets[sv->queue.front()];
+        // refuse jobs that could never fit, wherever they are in the queue
+        for (auto q = sv->queue.begin(); q != sv->queue.end();) {
+          Ticket& t = sv->tickets[*q];
+          if (t.footprint <= budget) {
+            ++q;
+            continue;
+          }
           t.status = KNNG_E_ADMIT;
           t.done = true;
           t.started = t.finished = clk::now();
-          sv->queue.pop_front();
+          q = sv->queue.erase(q);
           sv->cv_done.notify_all();
         }
-        while (!sv->queue.empty() && int(batch.size()) < sv->prm.max_batch_jobs) {
-          const Ticket& t = sv->tickets[sv->queue.front()];
-          if (sv->in_use + fp + t.footprint > budget) break;
-          fp += t.footprint;
-          batch.push_back(sv->queue.front());
-          sv->queue.pop_front();
+        // FIFO with bounded backfill: a job that does not fit yet is passed
+        // over by later jobs that do, until it has been passed over
+        // kMaxBypass times; from then on nothing behind it is admitted, so the
+        // memory that frees up goes to it.
+        for (auto q = sv->queue.begin(); q != sv->queue.end() && int(batch.size()) < sv->prm.max_batch_jobs;) {
+          Ticket& t = sv->tickets[*q];
+          if (sv->in_use + fp + t.footprint <= budget) {
+            fp += t.footprint;
+            batch.push_back(*q);
+            q = sv->queue.erase(q);
+            continue;
+          }
+          if (t.bypassed >= kMaxBypass) break;
+          ++q;
+        }
+        if (!batch.empty()) {
+          // every job still queued that arrived before an admitted one was passed over
+          clk::time_point latest = sv->tickets[batch.front()].submitted;
+          for (uint64_t id : batch) latest = std::max(latest, sv->tickets[id].submitted);
+          for (uint64_t id : sv->queue) {
+            Ticket& t = sv->tickets[id];
+            if (t.submitted >= latest) break;
+            ++t.bypassed;
+          }
         }
         if (!batch.empty()) break;
         sv->cv_work.wait(lk);
@@ -197,13 +226,22 @@ int knng_poll(knng_server* sv, uint64_t ticket, knng_result* r) {
 int knng_wait(knng_server* sv, uint64_t ticket, double timeout_s, knng_result* r) {
   if (!sv) return KNNG_E_ARGS;
   std::unique_lock<std::mutex> lk(sv->mu);
-  auto it = sv->tickets.find(ticket);
-  if (it == sv->tickets.end()) return KNNG_E_NOTFOUND;
   const auto until = clk::now() + std::chrono::duration_cast<clk::duration>(std::chrono::duration<double>(timeout_s));
-  while (!it->second.done)
-    if (sv->cv_done.wait_until(lk, until) == std::cv_status::timeout && !it->second.done) return KNNG_E_TIMEOUT;
-  fill_result(it->second, r);
-  return KNNG_OK;
+  for (;;) {
+    // looked up again after every wake-up: another thread may have released
+    // the ticket while this one waited without the lock
+    auto it = sv->tickets.find(ticket);
+    if (it == sv->tickets.end()) return KNNG_E_NOTFOUND;
+    if (it->second.done) {
+      fill_result(it->second, r);
+      return KNNG_OK;
+    }
+    if (sv->cv_done.wait_until(lk, until) == std::cv_status::timeout) {
+      it = sv->tickets.find(ticket);
+      if (it == sv->tickets.end()) return KNNG_E_NOTFOUND;
+      if (!it->second.done) return KNNG_E_TIMEOUT;
+    }
+  }
 }
 
 int knng_release(knng_server* sv, uint64_t ticket) {

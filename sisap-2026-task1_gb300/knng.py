@@ -40,7 +40,8 @@ class Params(C.Structure):
         ("rate_diff_tol", C.c_float), ("quant_mode", C.c_int), ("join_mode", C.c_int),
         ("row_order", C.c_int), ("seed", C.c_uint32), ("device", C.c_int), ("autotune", C.c_int),
         ("use_graph", C.c_int), ("gram_mode", C.c_int), ("init_mode", C.c_int), ("join_cache", C.c_int),
-        ("block_size", C.c_int), ("bridges", C.c_int),
+        ("block_size", C.c_int), ("bridges", C.c_int), ("wait_limit", C.c_int), ("join_ctas_per_sm", C.c_int),
+        ("join_cblock", C.c_int),
     ]
 
 
@@ -418,6 +419,16 @@ def init_graph_noalloc(codes, perm, leaf_flag, num_trees=16, leaf_size=64, k_bui
     n, d = codes.shape
     ids = torch.empty((n, k_build), dtype=torch.int32, device=codes.device) if ids is None else ids
     scores = torch.empty((n, k_build), dtype=torch.int32, device=codes.device) if scores is None else scores
+    # buffers from a foreign pool are written by the kernels as they are: check
+    # every shape, type, layout and device before the call
+    want = [(codes, (n, d), torch.int8, "codes"), (perm, (num_trees, n), torch.int32, "perm"),
+            (leaf_flag, (num_trees, n), torch.uint8, "leaf_flag"), (ids, (n, k_build), torch.int32, "ids"),
+            (scores, (n, k_build), torch.int32, "scores")]
+    for t, shape, dtype, name in want:
+        if (tuple(t.shape) != shape or t.dtype != dtype or not t.is_contiguous() or not t.is_cuda
+                or t.device != codes.device):
+            raise KnngError(-1, f"init_graph_noalloc: {name} must be a contiguous {dtype} CUDA tensor of shape "
+                                f"{shape} on {codes.device}, got {tuple(t.shape)} {t.dtype} on {t.device}")
     _ready(codes, perm, leaf_flag)
     st = lib().knng_init_graph_noalloc(_ptr(codes), n, d, num_trees, leaf_size, k_build, seed, _ptr(perm),
                                        _ptr(leaf_flag), _ptr(ids), _ptr(scores), _stream_ptr(stream))

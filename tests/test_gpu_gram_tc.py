@@ -60,3 +60,38 @@ def test_tc_full_build_equals_dp4a(knng_mod):
     np.testing.assert_array_equal(ka, kb)
     np.testing.assert_array_equal(da, db)
     assert sa.iterations == sb.iterations
+
+
+@pytest.mark.parametrize("d", [1024, 256])
+def test_tc_wait_timeout_reports_and_context_recovers(knng_mod, d):
+    """The tensor-core Gram's mbarrier waits are bounded.  With the limit set to
+    give up at once every wait for tensor-core work fails (d = 1024: in the
+    staging loop, d = 256: at the end of each tile); the kernel flags the
+    timeout, the whole block stops, the committed MMAs are drained with the
+    full limit and tensor memory is freed.  The call returns KNNG_E_TIMEOUT,
+    and builds afterwards -- in a new context and in the same process -- are
+    exact again."""
+    import torch
+
+    knng = knng_mod
+    x = synth.mixture(3000, d, 30, seed=91)
+    codes_ref, _ = oracle.quantize(x)
+    prm = oracle.params(threads=1, tie_mode=oracle.TIE_STABLE, jacobi=1)
+    perm_ref, lf_ref, _ = oracle.forest(codes_ref, prm)
+    ids_ref, sc_ref = oracle.init_graph(codes_ref, perm_ref, lf_ref, prm)
+    codes = torch.from_numpy(codes_ref).cuda()
+    perm, lf = torch.from_numpy(perm_ref).cuda(), torch.from_numpy(lf_ref).cuda()
+    with knng.Context(gram_mode=knng.GRAM_TCGEN05, wait_limit=-1) as ctx:
+        with pytest.raises(knng.KnngError) as e:
+            ctx.init_graph(codes, perm, lf)
+        assert e.value.status == -5  # KNNG_E_TIMEOUT
+        with pytest.raises(knng.KnngError) as e2:
+            ctx.build(x)
+        assert e2.value.status == -5
+    torch.cuda.synchronize()  # the device is still usable
+    with knng.Context(gram_mode=knng.GRAM_TCGEN05) as ctx:
+        ids, sc = ctx.init_graph(codes, perm, lf)
+        np.testing.assert_array_equal(sc.cpu().numpy(), sc_ref)
+        np.testing.assert_array_equal(ids.cpu().numpy(), ids_ref)
+        k, dd, st = ctx.build(x)
+        assert st.iterations >= 1 and k.min() >= 1

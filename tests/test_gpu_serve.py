@@ -93,3 +93,36 @@ def test_poll_and_concurrent_submitters(knng_mod):
     for k, (kn, dd, r) in done.items():
         np.testing.assert_array_equal(kn, solo[k][0])
         np.testing.assert_array_equal(dd, solo[k][1])
+
+
+def test_admission_backfills_past_a_job_that_does_not_fit(knng_mod):
+    """Two slots; a long job runs; the next queued job needs the whole budget,
+    so it must wait for the memory to free up, and a small job queued behind it
+    is admitted on the idle slot meanwhile instead of waiting behind it."""
+    knng = knng_mod
+    fp = knng.lib().knng_footprint_bytes
+    first = synth.mixture(40000, 1024, 400, seed=41)   # runs first, on slot 0
+    big = synth.mixture(60000, 1024, 600, seed=42)     # fits only when nothing else runs
+    small = synth.mixture(1500, 1024, 15, seed=43)     # fits next to the first job
+    b_big, b_first, b_small = fp(None, 60000, 1024, 0), fp(None, 40000, 1024, 0), fp(None, 1500, 1024, 0)
+    budget = b_big + 1  # the big job runs alone; the first and the small job fit together
+    assert b_first + b_small <= budget and b_small + b_big > budget
+    with knng.Context() as ctx:
+        solo_small = ctx.build(small)[:2]
+    with knng.Server(slots=2, mem_budget_gb=budget / 1e9) as sv:
+        t0 = time.perf_counter()
+        tf = sv.submit(first)
+        time.sleep(0.05)  # the first job is admitted and running
+        tb = sv.submit(big)
+        t_big = time.perf_counter()
+        ts = sv.submit(small)
+        t_small = time.perf_counter()
+        _, _, rf = sv.wait(tf)
+        _, _, rb = sv.wait(tb)
+        ks, ds, rs = sv.wait(ts)
+    assert rf.status == rb.status == rs.status == 0
+    big_start = t_big + rb.queued_s
+    small_done = t_small + rs.latency_s
+    assert small_done <= big_start + 1e-3, (small_done - t0, big_start - t0)
+    np.testing.assert_array_equal(ks, solo_small[0])
+    np.testing.assert_array_equal(ds, solo_small[1])
