@@ -12,6 +12,11 @@ library's stream); `e2e` is the same build through knng_build with pinned host
 rows in and host knns/dists out, copies inside the timed region.  The inputs
 (26 GB at 6.35M x 1024) are far larger than L2, so no flush is needed.
 
+At N = 1 the line also carries `batched` (64 independent jobs in one
+knng_build_batch call against the same jobs built one after another) and
+`serving` (Poisson arrivals through the serving loop: jobs/s, p50/p99
+latency); `--config batched|serving` prints either as a line of its own.
+
 Several GPUs run independent replicas (the build does not shard): each rank
 builds its own dataset of the configured size; value = all ranks' vectors /
 max-over-ranks time.
@@ -154,25 +159,15 @@ def recall_sample(x, knns, rows=10_000, seed=7):
     """recall@15 of exported knns on a seeded row sample vs exact fp64 brute force (GPU)."""
     import torch
 
+    import evaluate
     import synth
 
     n = x.shape[0]
     g = torch.Generator().manual_seed(seed)
-    idx = torch.randperm(n, generator=g)[: min(rows, n)].to(x.device)
-    gt = []
-    for s in range(0, len(idx), 500):
-        q = idx[s:s + 500]
-        sims = x[q] @ x.T  # fp32 pass, then fp64 rescoring of the best 64
-        sims[torch.arange(len(q), device=x.device), q] = -float("inf")
-        cand = sims.topk(64, dim=1).indices
-        exact = torch.einsum("bd,bmd->bm", x[q].double(), x[cand].double())
-        exact[cand == q[:, None]] = -float("inf")
-        order = exact.argsort(dim=1, descending=True, stable=True)[:, :15]
-        gt.append(torch.gather(cand, 1, order).cpu())
-        del sims
-    gt = torch.cat(gt).numpy()
+    idx = torch.randperm(n, generator=g)[: min(rows, n)].numpy()
+    gt = evaluate.sample_knn(x, idx, 15)
     kh = knns.cpu().numpy() if hasattr(knns, "cpu") else knns
-    return synth.recall_at_k(kh, gt, rows=idx.cpu().numpy())
+    return synth.recall_at_k(kh, gt, rows=idx)
 
 
 def cpu_port_step(threads, sample=CPU_SAMPLE, seed=4242, want=False):
@@ -204,6 +199,39 @@ def recall_parity(x_np, ref_knns, dev):
     r_ref = recall_sample(x, torch.from_numpy(ref_knns), rows=x.shape[0])
     r_gpu = recall_sample(x, kg, rows=x.shape[0])
     return {"n": int(x.shape[0]), "reference_port": r_ref, "gpu": r_gpu, "gap_pt": 100 * (r_ref - r_gpu)}
+
+
+def same_sample_gpu(dev, steps, warmup, sample=CPU_SAMPLE, seed=4242):
+    """The GPU build timed on exactly the rows the reference arm builds (the
+    bounded CPU sample: same generator, size and seed): device-resident
+    vectors/s and, through knng_build with pinned host rows in and host
+    knns/dists out, end-to-end vectors/s.  Same N on both sides, so the ratio
+    to the reference arm is like for like."""
+    import torch
+
+    import knng
+    import synth
+
+    n, d, c = sample
+    xh_np = synth.mixture(n, d, c, seed=seed)
+    x = torch.from_numpy(xh_np).to(dev)
+    xh = torch.from_numpy(xh_np).pin_memory()
+    kh = torch.empty((n, 15), dtype=torch.int32, pin_memory=True)
+    dh = torch.empty((n, 15), dtype=torch.float32, pin_memory=True)
+    dev_s, e2e_s = [], []
+    with knng.Context() as ctx:
+        for _ in range(warmup):
+            ctx.build(x)
+            ctx.build(xh, kh, dh)
+        for _ in range(steps):
+            st = knng.Stats()
+            ctx.build(x, None, None, st)
+            dev_s.append(st.device_s)
+            st = knng.Stats()
+            ctx.build(xh, kh, dh, st)
+            e2e_s.append(st.device_s)
+    return {"value": n / statistics.mean(dev_s), "e2e": n / statistics.mean(e2e_s), "unit": "vectors/s",
+            "sample": f"{n} x {d} rows, {c} centres, seed {seed}: the reference arm's own sample", "steps": steps}
 
 
 def cpu_ref_step(threads, sample=CPU_SAMPLE, seed=4242):
@@ -286,12 +314,11 @@ def _job_specs(count, lo, hi, dims, seed):
     return [(int(n), int(d)) for n, d in zip(ns, ds)]
 
 
-def run_batched(args):
+def measure_batched(steps, warmup, seq_passes):
     """64 independent jobs (n log-uniform in [5k, 200k], d in {384, 768, 1024}):
     one knng_build_batch call per step against the same jobs as 64 plain
-    knng_build calls.  value = batched jobs/s; every job's output is checked
-    bit-identical between the two."""
-    import numpy as np
+    knng_build calls.  Returns batched and sequential jobs/s (device-timed);
+    every job's output is checked bit-identical between the two."""
     import torch
 
     import knng
@@ -303,12 +330,12 @@ def run_batched(args):
     torch.cuda.synchronize()
     rows = sum(n for n, _ in specs)
     with knng.Context() as ctx:
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             res, _ = ctx.build_batch(xs)
         bt = []
         launches = 0
         with ClockSampler(0) as clk:
-            for _ in range(args.steps):
+            for _ in range(steps):
                 st = knng.Stats()
                 res, st = ctx.build_batch(xs, st)
                 bt.append(st.device_s)
@@ -317,32 +344,43 @@ def run_batched(args):
             ctx.build(x)  # warm the plain path too (autotune buckets, buffers)
         seq = []
         same = True
-        for _ in range(max(1, args.steps // 2)):
+        for _ in range(seq_passes):
             tot = 0.0
             for j, x in enumerate(xs):
                 k, d_, st1 = ctx.build(x)
                 tot += st1.device_s
                 same &= bool(torch.equal(k, res[j][0]) and torch.equal(d_, res[j][1]))
             seq.append(tot)
+    del xs
+    torch.cuda.empty_cache()
     b_js = 64 / statistics.mean(bt)
     s_js = 64 / statistics.mean(seq)
-    line = {"metric": "jobs/s (64 independent kNN-graph builds, batched)", "value": b_js, "unit": "jobs/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(bt),
+    return {"workload": "64 jobs, n log-uniform [5k, 200k], d in {384, 768, 1024}", "rows": rows,
+            "jobs_per_s": b_js, "ms_per_step": 1e3 * statistics.mean(bt), "steps": steps,
+            "sequential_plain_jobs_per_s": s_js, "batched_over_sequential": b_js / s_js,
+            "identical_to_plain": same, "vectors_per_s": rows / statistics.mean(bt), "clocks": clk.summary(),
+            "gpu_launches": launches}
+
+
+def run_batched(args):
+    b = measure_batched(args.steps, args.warmup, max(1, args.steps // 2))
+    line = {"metric": "jobs/s (64 independent kNN-graph builds, batched)", "value": b["jobs_per_s"], "unit": "jobs/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": b["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8/int32",
             "data": "synthetic (seeded Gaussian mixtures, one per job)",
-            "config": {"workload": "batched builds: 64 jobs, n log-uniform [5k, 200k], d in {384, 768, 1024}",
-                       "rows": rows, "l2": "inputs far larger than L2"},
-            "sequential_plain_jobs_per_s": s_js, "batched_over_sequential": b_js / s_js,
-            "identical_to_plain": same, "vectors_per_s": rows / statistics.mean(bt),
-            "clocks": clk.summary(), "gpu_launches": launches}
+            "config": {"workload": "batched builds: " + b["workload"], "rows": b["rows"],
+                       "l2": "inputs far larger than L2"},
+            "sequential_plain_jobs_per_s": b["sequential_plain_jobs_per_s"],
+            "batched_over_sequential": b["batched_over_sequential"], "identical_to_plain": b["identical_to_plain"],
+            "vectors_per_s": b["vectors_per_s"], "clocks": b["clocks"], "gpu_launches": b["gpu_launches"]}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_serving(args):
+def measure_serving(count, slots):
     """Poisson arrivals (mean 4 jobs/s) of builds with n log-uniform in [10k, 2M],
     d = 1024, rows resident in HBM; the server admits them by footprint against
-    180 GB and batches them continuously.  Reports jobs/s and p50/p99 latency
+    180 GB and batches them continuously.  Returns jobs/s and p50/p99 latency
     next to the same jobs built one after another."""
     import numpy as np
     import torch
@@ -351,7 +389,6 @@ def run_serving(args):
     import synth
 
     dev = torch.device("cuda", 0)
-    count = args.serve_jobs
     specs = _job_specs(count, 10_000, 2_000_000, (1024,), seed=5003)
     xs = [synth.mixture_torch(n, d, max(1, n // 100), seed=5000 + j, device=dev) for j, (n, d) in enumerate(specs)]
     torch.cuda.synchronize()
@@ -366,7 +403,7 @@ def run_serving(args):
             seq_s += st.device_s
             if j < 4:
                 solo[j] = (k, d_)
-    with knng.Server(slots=args.slots, mem_budget_gb=180.0) as sv:
+    with knng.Server(slots=slots, mem_budget_gb=180.0) as sv:
         sv.wait(sv.submit(xs[0]))  # warm the workers
         tickets = [None] * count
         t0 = time.perf_counter()
@@ -377,17 +414,29 @@ def run_serving(args):
             outs = [sv.wait(t, 1200.0) for t in tickets]
             t_end = time.perf_counter()
     lat = sorted(r.latency_s for _, _, r in outs)
+    mean_batch = float(np.mean([r.batch_jobs for _, _, r in outs]))
     same = all(torch.equal(outs[j][0], solo[j][0]) and torch.equal(outs[j][1], solo[j][1]) for j in solo)
-    arrive_span = float(np.sum(gaps))
-    line = {"metric": "jobs/s (serving, Poisson 4 jobs/s, n log-uniform [10k, 2M])", "value": count / (t_end - t0),
-            "unit": "jobs/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * (t_end - t0),
+    del xs, outs
+    torch.cuda.empty_cache()
+    return {"workload": f"{count} jobs, Poisson mean 4/s, n log-uniform [10k, 2M], d = 1024, 180 GB budget",
+            "slots": slots, "rows": int(sum(n for n, _ in specs)), "arrival_span_s": float(np.sum(gaps)),
+            "jobs_per_s": count / (t_end - t0), "wall_s": t_end - t0,
+            "p50_latency_s": lat[len(lat) // 2], "p99_latency_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+            "mean_batch_jobs": mean_batch, "sequential_plain_jobs_per_s": count / seq_s, "identical_to_plain": same,
+            "clocks": clk.summary()}
+
+
+def run_serving(args):
+    sv = measure_serving(args.serve_jobs, args.slots)
+    line = {"metric": "jobs/s (serving, Poisson 4 jobs/s, n log-uniform [10k, 2M])", "value": sv["jobs_per_s"],
+            "unit": "jobs/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * sv["wall_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8/int32",
             "data": "synthetic (seeded Gaussian mixtures, one per job)",
-            "config": {"workload": f"serving loop: {count} jobs, Poisson mean 4/s, d=1024, 180 GB budget",
-                       "slots": args.slots, "rows": int(sum(n for n, _ in specs)), "arrival_span_s": arrive_span},
-            "p50_latency_s": lat[len(lat) // 2], "p99_latency_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
-            "mean_batch_jobs": float(np.mean([r.batch_jobs for _, _, r in outs])),
-            "sequential_plain_jobs_per_s": count / seq_s, "identical_to_plain": same, "clocks": clk.summary()}
+            "config": {"workload": "serving loop: " + sv["workload"], "slots": sv["slots"], "rows": sv["rows"],
+                       "arrival_span_s": sv["arrival_span_s"]},
+            "p50_latency_s": sv["p50_latency_s"], "p99_latency_s": sv["p99_latency_s"],
+            "mean_batch_jobs": sv["mean_batch_jobs"], "sequential_plain_jobs_per_s": sv["sequential_plain_jobs_per_s"],
+            "identical_to_plain": sv["identical_to_plain"], "clocks": sv["clocks"]}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -497,6 +546,8 @@ def run_gpu(args):
                         "sketch plus R rows per row, an upper bound the kernel avoids by deduplicating"}
     # ---- recall on a seeded sample
     rec = recall_sample(x, knns, rows=args.recall_rows) if args.recall_rows > 0 and rank == 0 else None
+    # ---- the same build on the reference arm's own sample rows (like-for-like N)
+    same = same_sample_gpu(dev, args.steps, max(1, args.warmup)) if rank == 0 and ws == 1 else None
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     parity = None
@@ -525,11 +576,19 @@ def run_gpu(args):
             "stage_s": {"quantize": last.quantize_s, "forest": last.forest_s, "init": last.init_s,
                         "join": last.join_s, "export": last.export_s},
             "recall@15": rec, "recall_rows": args.recall_rows, "recall_parity_100k": parity,
+            "value_same_config": same["value"] if same else None, "same_config": same,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clk.summary(), "gpu_launches": launches, "wall_s": wall,
         }
-        print(json.dumps(line), flush=True)
     ctx.close()
+    del x, knns, dists
+    torch.cuda.empty_cache()
+    # ---- the batched and served forms (one GPU: rank 0 at N = 1)
+    if rank == 0 and ws == 1 and not args.skip_forms:
+        line["batched"] = measure_batched(min(args.steps, 5), 2, 1)
+        line["serving"] = measure_serving(args.serve_jobs, args.slots)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     grp.close()
     return 0
 
@@ -550,6 +609,8 @@ def main():
     ap.add_argument("--recall-rows", type=int, default=10_000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-forms", action="store_true",
+                    help="leave the batched and serving measurements out of the default line")
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="dram read+write bytes per join launch from an ncu capture, scaled to this workload")
     args = ap.parse_args()

@@ -46,6 +46,7 @@ enum { KNNG_JOIN_JACOBI = 0, KNNG_JOIN_INPLACE = 1 };
 enum { KNNG_ORDER_NATURAL = 0, KNNG_ORDER_LEAF = 1 };
 enum { KNNG_GRAM_DP4A = 0, KNNG_GRAM_TCGEN05 = 1 };
 enum { KNNG_INIT_FOREST = 0, KNNG_INIT_RANDOM = 1, KNNG_INIT_BLOCK = 2 };
+enum { KNNG_SKETCH_SIGN = 0, KNNG_SKETCH_HYPERPLANE = 1 };
 
 /* Build parameters.  Defaults (knng_default_params) are the reference's
  * compile-time constants, src/main.cpp:19-29. */
@@ -89,6 +90,11 @@ typedef struct knng_params {
                             Hamming candidates in flight) for every iteration and for
                             knng_join_iter.  Results are identical for every variant. */
   int join_cblock;
+  int sketch_mode;       /* KNNG_SKETCH_SIGN: one sign bit per coordinate, d bits per row, as
+                            src/main.cpp:182-190 (default).  KNNG_SKETCH_HYPERPLANE: 128 bits per
+                            row, the signs of the int8 codes projected on 128 integer
+                            hyperplanes drawn from `seed` (the README's random-hyperplane
+                            sketch, README.md:33-34; no output of the reference to match) */
 } knng_params;
 
 /* Per-build timings and convergence record (seconds, device-timed). */
@@ -114,6 +120,9 @@ typedef struct knng_stats {
   int join_cblock;
   int graph_used;         /* NN-Descent phase ran as a CUDA graph */
   int64_t join_distinct[64]; /* distinct two-hop candidates per iteration (all rows) */
+  int64_t join_skipped[64];  /* rows copied through per iteration because neither their list nor
+                                any neighbour's list changed in the previous one (double-buffered
+                                iterations: their result is provably their current list) */
 } knng_stats;
 
 /* One job of a batch (knng_build_batch).  Inputs as for knng_build; status
@@ -227,6 +236,16 @@ const char* knng_last_error(const knng_ctx* ctx);
 int knng_quantize(const float* x_dev, int64_t n, int d, int quant_mode, int8_t* codes_dev,
                   uint64_t* sketch_dev, void* stream);
 
+/* Optional sketch (no counterpart in src/main.cpp, whose sketch is the sign
+ * of each coordinate; its README.md:33-34 describes random hyperplanes):
+ * sketch_dev[n][2] receives 128 bits per row, bit k set iff the exact int32
+ * projection of the row's int8 codes on seeded integer hyperplane k is > 0.
+ * Plane k, coordinate j: h = SplitMix64((seed << 32) ^ (k << 10 | j)),
+ * value = sum over the 4 low bytes b of h of (b >> 2) - 32.  codes_dev must be
+ * 16-byte aligned; d a multiple of 128 in [128, 1024]. */
+int knng_sketch_hyperplane(const int8_t* codes_dev, int64_t n, int d, uint32_t seed, uint64_t* sketch_dev,
+                           void* stream);
+
 /* a2/a3, src/main.cpp:47-99, 205-232: RP forest.  perm_dev[t*n + p] is the id
  * at position p of tree t's leaf order; leaf_flag_dev[t*n + p] = 1 where a
  * leaf starts.  replay (host, may be NULL) holds n_replay internal nodes as
@@ -244,7 +263,9 @@ int knng_init_graph(knng_ctx* ctx, const int8_t* codes_dev, int64_t n, int d,
                     int32_t* scores_dev);
 
 /* a5, src/main.cpp:324-430: one NN-Descent iteration reading ids_in/scores_in
- * and writing ids_out/scores_out (the same pointers = in place).  The rerank
+ * and writing ids_out/scores_out (the same pointers = in place).  sketch_dev
+ * holds the context's sketch_mode's sketches: [n][d/64] sign sketches, or
+ * [n][2] hyperplane sketches.  The rerank
  * set is the best k_build*rerank_mult candidates by (hamming desc, sequence
  * position asc), visited in that order.  *updates receives the number of
  * positions whose id changed. */

@@ -82,6 +82,7 @@ struct oracle_params {
   int jacobi;             // 0 = in place (reference), 1 = double buffered
   int threads;            // OpenMP threads (<= 0: leave the runtime default)
   uint32_t seed;          // 1337, src/main.cpp:210 and :271
+  int sketch_mode;        // 0: the reference's coordinate-sign sketch; 1: 128 seeded hyperplanes
 };
 
 void oracle_default_params(oracle_params* p) {
@@ -98,6 +99,7 @@ void oracle_default_params(oracle_params* p) {
   p->jacobi = 0;
   p->threads = 1;
   p->seed = 1337;
+  p->sketch_mode = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -136,6 +138,49 @@ void oracle_quantize(const float* x, int64_t n, int d, int quant_mode, int8_t* c
       }
       if (clamped > 0) b[k / 64] |= (1ULL << (k % 64));
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Optional sketch: 128 seeded random hyperplanes (the README's "128-bit
+// random-hyperplane sketches", README.md:33-34; src/main.cpp itself keeps the
+// coordinate-sign sketch above, so this mode has no reference output and is
+// pinned only by this restatement and a numpy one in the tests).
+//   plane k, coordinate j:  h = SplitMix64((seed << 32) ^ (k << 10 | j)),
+//     g = sum over the 4 low bytes b of h of (b >> 2) - 32  (in [-128, 124],
+//     a sum of four uniforms: close to Gaussian);
+//   bit k of row i = (sum_j q_ij * g_kj > 0), exact in int32; bit k % 64 of
+//   word k / 64, two words per row.
+// The Hamming score of two rows stays 1024 - popcount over their words.
+static uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+int8_t oracle_plane_value(uint32_t seed, int k, int j) {
+  const uint64_t h = splitmix64((uint64_t(seed) << 32) ^ uint64_t((uint32_t(k) << 10) | uint32_t(j)));
+  int v = 0;
+  for (int b = 0; b < 4; ++b) v += int((h >> (8 * b)) & 0xff) / 4 - 32;
+  return int8_t(v);
+}
+
+void oracle_hyperplane_sketch(const int8_t* codes, int64_t n, int d, uint32_t seed, uint64_t* sketch) {
+  std::vector<int8_t> g(size_t(128) * d);
+  for (int k = 0; k < 128; ++k)
+    for (int j = 0; j < d; ++j) g[size_t(k) * d + j] = oracle_plane_value(seed, k, j);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const int8_t* q = codes + i * d;
+    uint64_t w[2] = {0, 0};
+    for (int k = 0; k < 128; ++k) {
+      int32_t dot = 0;
+      for (int j = 0; j < d; ++j) dot += int32_t(q[j]) * int32_t(g[size_t(k) * d + j]);
+      if (dot > 0) w[k / 64] |= 1ull << (k % 64);
+    }
+    sketch[i * 2] = w[0];
+    sketch[i * 2 + 1] = w[1];
   }
 }
 
@@ -522,15 +567,19 @@ int oracle_build(const float* x, int64_t n, int d, const oracle_params* prm, int
   using clk = std::chrono::steady_clock;
   if (n <= 1 || d <= 0 || d % 64 != 0) return -1;
   const int K = prm->k_build;
-  const int words = d / 64;
+  const int qwords = d / 64;
+  const int words = prm->sketch_mode == 1 ? 2 : qwords;
   std::vector<int8_t> codes(size_t(n) * d);
+  std::vector<uint64_t> qsk(size_t(n) * qwords);
   std::vector<uint64_t> sk(size_t(n) * words);
   oracle_stats local{};
   if (!st) st = &local;
   std::memset(st, 0, sizeof(*st));
   set_threads(prm->threads);
   auto t0 = clk::now();
-  oracle_quantize(x, n, d, prm->quant_mode, codes.data(), sk.data(), words);
+  oracle_quantize(x, n, d, prm->quant_mode, codes.data(), qsk.data(), qwords);
+  if (prm->sketch_mode == 1) oracle_hyperplane_sketch(codes.data(), n, d, prm->seed, sk.data());
+  else sk.swap(qsk);
   auto t1 = clk::now();
   std::vector<int32_t> perm(size_t(prm->num_trees) * n);
   std::vector<uint8_t> lf(size_t(prm->num_trees) * n);

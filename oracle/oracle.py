@@ -31,7 +31,7 @@ class Params(C.Structure):
         ("rerank_mult", C.c_int), ("leaf_size", C.c_int), ("max_iterations", C.c_int),
         ("early_stop_rate", C.c_float), ("rate_diff_tol", C.c_float),
         ("quant_mode", C.c_int), ("tie_mode", C.c_int), ("jacobi", C.c_int),
-        ("threads", C.c_int), ("seed", C.c_uint32),
+        ("threads", C.c_int), ("seed", C.c_uint32), ("sketch_mode", C.c_int),
     ]
 
 
@@ -76,6 +76,9 @@ def lib():
         L.oracle_join_iter.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int64, C.c_int, P(Params),
                                        C.c_void_p, C.c_void_p]
         L.oracle_join_iter.restype = C.c_int64
+        L.oracle_hyperplane_sketch.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_uint32, C.c_void_p]
+        L.oracle_plane_value.argtypes = [C.c_uint32, C.c_int, C.c_int]
+        L.oracle_plane_value.restype = C.c_int8
         L.oracle_export.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         L.oracle_build.argtypes = [C.c_void_p, C.c_int64, C.c_int, P(Params), C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, P(Stats)]
@@ -103,6 +106,19 @@ def quantize(x, quant_mode=QUANT_TRUNC):
     sk = np.empty((n, words), np.uint64)
     lib().oracle_quantize(_ptr(x), n, d, quant_mode, _ptr(codes), _ptr(sk), words)
     return codes, sk
+
+
+def hyperplane_sketch(codes, seed=1337):
+    """128-bit sketches from 128 seeded integer hyperplanes: (n, 2) uint64."""
+    codes = np.ascontiguousarray(codes)
+    n, d = codes.shape
+    sk = np.empty((n, 2), np.uint64)
+    lib().oracle_hyperplane_sketch(_ptr(codes), n, d, seed, _ptr(sk))
+    return sk
+
+
+def plane_value(seed, k, j):
+    return int(lib().oracle_plane_value(seed, k, j))
 
 
 def forest(codes, prm=None, log_pivots=False):

@@ -102,7 +102,7 @@ struct knng_ctx {
   cudaEvent_t copied[2] = {}, freed[2] = {};
   cudaEvent_t itev[kMaxIterEvents] = {};
   std::string last_error;
-  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs, cache;
+  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs, cache, hsketch, rowflags;
   // join phase captured as a CUDA graph, reused while the launch key matches
   cudaGraphExec_t join_graph = nullptr;
   std::vector<uintptr_t> join_graph_key;
@@ -111,8 +111,13 @@ struct knng_ctx {
   std::map<std::pair<int, int>, JoinCfg> tuned;
   std::vector<knng_ctx*> subs;  // contexts of the second and later dimension groups of a batch
   std::vector<DevBuf*> buffers() {
-    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs, &cache};
+    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs, &cache,
+            &hsketch, &rowflags};
   }
+  // the sketches the join scores and their 64-bit words per row
+  bool hyperplane() const { return prm.sketch_mode == KNNG_SKETCH_HYPERPLANE; }
+  const uint64_t* join_sketch() const { return hyperplane() ? hsketch.as<uint64_t>() : sketch.as<uint64_t>(); }
+  int sketch_words(int d) const { return hyperplane() ? 2 : d / 64; }
 };
 
 namespace {
@@ -152,6 +157,8 @@ int check_params(knng_ctx* c, const knng_params& p) {
   if (p.join_ctas_per_sm != 0 &&
       (p.join_ctas_per_sm < 3 || p.join_ctas_per_sm > 4 || (p.join_cblock != 2 && p.join_cblock != 4 && p.join_cblock != 8)))
     return set_error(c, KNNG_E_ARGS, "join_ctas_per_sm must be 0, or 3 or 4 with join_cblock 2, 4 or 8");
+  if (p.sketch_mode != KNNG_SKETCH_SIGN && p.sketch_mode != KNNG_SKETCH_HYPERPLANE)
+    return set_error(c, KNNG_E_ARGS, "bad sketch_mode");
   return KNNG_OK;
 }
 
@@ -336,9 +343,9 @@ JoinCfg autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int3
     float best_ms = 1e30f;
     for (const auto& cf : cand) {
       cudaEventRecord(c->jev[0], c->stream);
-      if (launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
+      if (launch_join(c->codes.as<int8_t>(), c->join_sketch(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
                       ids[1], scs[1], order, scratch_counters, c->num_sms, c->stream, nullptr, ctl, cf.first,
-                      cf.second) != cudaSuccess)
+                      cf.second, c->sketch_words(d)) != cudaSuccess)
         return false;
       cudaEventRecord(c->jev[1], c->stream);
       cudaEventSynchronize(c->jev[1]);
@@ -354,9 +361,9 @@ JoinCfg autotune_join(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int3
   best.late = best.early;
   if (cache_ctl) {
     if (cudaMemsetAsync(cache_ctl->cache_cnt, 0, size_t(N) * 4, c->stream) != cudaSuccess ||
-        launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
+        launch_join(c->codes.as<int8_t>(), c->join_sketch(), N, d, K, K * p.rerank_mult, ids[0], scs[0],
                     ids[1], scs[1], order, scratch_counters, c->num_sms, c->stream, nullptr, &cached,
-                    best.early.first, best.early.second) != cudaSuccess ||
+                    best.early.first, best.early.second, c->sketch_words(d)) != cudaSuccess ||
         !sweep(&cached, &best.late))
       return best;
   }
@@ -376,12 +383,18 @@ cudaError_t join_phase(knng_ctx* c, int64_t N, int d, int32_t* const ids[2], int
   int cur = 0;
   for (int it = 0; it < p.max_iterations; ++it) {
     const int nxt = jac ? 1 - cur : cur;
+    JoinCtl ci = ctl;  // this iteration's row-change flags: read the previous iteration's, write its own
+    if (jac && c->rowflags.p) {
+      ci.chg_in = c->rowflags.as<uint8_t>(size_t(it & 1) * size_t(N));
+      ci.chg_out = c->rowflags.as<uint8_t>(size_t((it + 1) & 1) * size_t(N));
+    }
     e = capture ? cudaEventRecordWithFlags(c->itev[2 * it], c->stream, cudaEventRecordExternal)
                 : cudaEventRecord(c->itev[2 * it], c->stream);
     if (e) return (*step = "iteration start event", e);
-    if ((e = launch_join(c->codes.as<int8_t>(), c->sketch.as<uint64_t>(), N, d, K, K * p.rerank_mult, ids[cur],
-                         scs[cur], ids[nxt], scs[nxt], order, counters + 4 * it, c->num_sms, c->stream, &jt, &ctl,
-                         (it < 2 ? cfg.early : cfg.late).first, (it < 2 ? cfg.early : cfg.late).second)))
+    if ((e = launch_join(c->codes.as<int8_t>(), c->join_sketch(), N, d, K, K * p.rerank_mult, ids[cur],
+                         scs[cur], ids[nxt], scs[nxt], order, counters + 8 * it, c->num_sms, c->stream, &jt, &ci,
+                         (it < 2 ? cfg.early : cfg.late).first, (it < 2 ? cfg.early : cfg.late).second,
+                         c->sketch_words(d))))
       return (*step = "join launch", e);
     e = capture ? cudaEventRecordWithFlags(c->itev[2 * it + 1], c->stream, cudaEventRecordExternal)
                 : cudaEventRecord(c->itev[2 * it + 1], c->stream);
@@ -415,7 +428,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   const size_t nk = size_t(N) * K;
   if ((e = c->codes.ensure(size_t(N) * d)) || (e = c->sketch.ensure(size_t(N) * W * 8)) ||
       (e = c->graph.ensure(nk * 16)) || (e = c->perm.ensure(size_t(T) * N * 4)) ||
-      (e = c->leaf_flag.ensure(size_t(T) * N)))
+      (e = c->leaf_flag.ensure(size_t(T) * N)) || (c->hyperplane() && (e = c->hsketch.ensure(size_t(N) * 16))))
     return cuda_fail(c, e, "device allocation");
   Scratch s;
   int st = ensure_scratch(c, N, &s, 0);
@@ -430,7 +443,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   };
   const size_t o_off = take(jb * 4), o_n = take(jb * 4), o_upd = take(jb * 8), o_done = take(jb * 4),
                o_prev = take(jb * 4), o_iters = take(jb * 4), o_flags = take(16), o_log = take(size_t(MI + 1) * jb * 8),
-               o_cnt = take(size_t(MI + 1) * 4 * 8);
+               o_cnt = take(size_t(MI + 1) * 8 * 8);
   if ((e = c->jobs.ensure(o))) return cuda_fail(c, e, "job table allocation");
   cudaStream_t str = c->stream;
   if ((e = cudaMemsetAsync(c->jobs.p, 0, o, str)) ||
@@ -455,6 +468,10 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   ctl.cache_cnt = nullptr;
   ctl.cache_cap = 0;
   ctl.row_limit = 0;  // every row
+  ctl.chg_in = nullptr;  // set per iteration by join_phase
+  ctl.chg_out = nullptr;
+  const bool skip_rows = p.join_mode == KNNG_JOIN_JACOBI && MI > 0;
+  if (skip_rows && (e = c->rowflags.ensure(size_t(2) * size_t(N)))) return cuda_fail(c, e, "row flag allocation");
   if (p.join_cache && MI > 0) {
     if ((e = c->cache.ensure(cache_bytes(N)))) return cuda_fail(c, e, "candidate cache allocation");
     char* cp = c->cache.as<char>();
@@ -465,13 +482,17 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     ctl.cache_cnt = reinterpret_cast<int*>(cp);
     ctl.cache_cap = kCacheCap;
   }
-  unsigned long long* tune_counters = ctl.counters + 4 * MI;
+  unsigned long long* tune_counters = ctl.counters + 8 * MI;
   int32_t* ids[2] = {c->graph.as<int32_t>(0), c->graph.as<int32_t>(nk * 8)};
   int32_t* scs[2] = {c->graph.as<int32_t>(nk * 4), c->graph.as<int32_t>(nk * 12)};
 
   cudaEventRecord(c->ev[0], str);
   for (int b = 0; b < J; ++b)
     if ((st = quantize_input(c, jobs[b].rows, jobs[b].n, d, jobs[b].on_dev, hoff[b]))) return st;
+  // the optional hyperplane sketch, from the codes (like the sign sketch, before buildtime starts)
+  if (c->hyperplane() &&
+      (e = launch_hyperplane_sketch(c->codes.as<int8_t>(), N, d, p.seed, c->hsketch.as<uint64_t>(), c->num_sms, str)))
+    return cuda_fail(c, e, "hyperplane sketch");
   cudaEventRecord(c->ev[1], str);
   int64_t levels = 0, leaves = 0;
   const bool forest_init = p.init_mode == KNNG_INIT_FOREST;
@@ -509,9 +530,11 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   tune_ctl.cache_cap = ctl.cache_cap;
   const JoinCfg cfg = autotune_join(c, N, d, ids, scs, order, tune_counters, ctl.cache_ids ? &tune_ctl : nullptr);
   cudaEventRecord(c->ev[3], str);
-  // every row starts the phase with an empty candidate cache
+  // every row starts the phase with an empty candidate cache, and counts as
+  // changed before the first iteration
   if (ctl.cache_cnt && (e = cudaMemsetAsync(ctl.cache_cnt, 0, size_t(N) * 4, str)))
     return cuda_fail(c, e, "candidate cache reset");
+  if (skip_rows && (e = cudaMemsetAsync(c->rowflags.p, 1, size_t(N), str))) return cuda_fail(c, e, "row flag reset");
   // NN-Descent, captured once per launch key and replayed
   bool graph_used = false;
   if ((e = join_prepare(K, K * p.rerank_mult, d, cfg.early.first, cfg.early.second)) ||
@@ -519,8 +542,9 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     return cuda_fail(c, e, (std::string("join variant: ") + join_variant_error()).c_str());
   const char* step = "";
   if (p.use_graph) {
-    const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->sketch.p), uintptr_t(c->graph.p),
+    const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->join_sketch()), uintptr_t(c->graph.p),
                                         uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(ctl.cache_ids),
+                                        uintptr_t(c->rowflags.p),
                                         uintptr_t(N), uintptr_t(d),
                                         uintptr_t(J), uintptr_t(o), uintptr_t(cfg.early.first), uintptr_t(cfg.early.second),
                                         uintptr_t(cfg.late.first), uintptr_t(cfg.late.second),
@@ -556,7 +580,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   // results of the control block
   std::vector<int> iters(jb);
   std::vector<long long> log(size_t(MI) * jb);
-  std::vector<unsigned long long> cnt(size_t(MI) * 4);
+  std::vector<unsigned long long> cnt(size_t(MI) * 8);
   int flags[2] = {0, 0};
   if ((e = cudaMemcpyAsync(iters.data(), ctl.job_iters, jb * 4, cudaMemcpyDeviceToHost, str)) ||
       (MI && (e = cudaMemcpyAsync(log.data(), ctl.upd_log, log.size() * 8, cudaMemcpyDeviceToHost, str))) ||
@@ -608,9 +632,10 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     for (int b = 0; b < J; ++b) u += log[size_t(it) * J + b];
     S.updates[it] = u;
     S.join_ms[it] = elapsed(c->itev[2 * it], c->itev[2 * it + 1]);
-    S.join_candidates[it] = int64_t(cnt[4 * it + 1]);
-    S.join_dots[it] = int64_t(cnt[4 * it + 2]);
-    S.join_distinct[it] = int64_t(cnt[4 * it + 3]);
+    S.join_candidates[it] = int64_t(cnt[8 * it + 1]);
+    S.join_dots[it] = int64_t(cnt[8 * it + 2]);
+    S.join_distinct[it] = int64_t(cnt[8 * it + 3]);
+    S.join_skipped[it] = int64_t(cnt[8 * it + 4]);
   }
   S.forest_levels = levels;
   S.leaves = leaves;
@@ -651,6 +676,7 @@ void knng_default_params(knng_params* p) {
   p->wait_limit = 0;
   p->join_ctas_per_sm = 0;
   p->join_cblock = 0;
+  p->sketch_mode = KNNG_SKETCH_SIGN;
 }
 
 const char* knng_status_string(int s) {
@@ -761,6 +787,17 @@ int knng_quantize(const float* x_dev, int64_t n, int d, int quant_mode, int8_t* 
   return e ? KNNG_E_CUDA : KNNG_OK;
 }
 
+int knng_sketch_hyperplane(const int8_t* codes_dev, int64_t n, int d, uint32_t seed, uint64_t* sketch_dev,
+                           void* stream) {
+  if (!codes_dev || !sketch_dev || n < 0 || (reinterpret_cast<uintptr_t>(codes_dev) & 15)) return KNNG_E_ARGS;
+  if (!dim_ok(d)) return KNNG_E_DIM;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return KNNG_E_CUDA;
+  const cudaError_t e = launch_hyperplane_sketch(codes_dev, n, d, seed, sketch_dev, sms, static_cast<cudaStream_t>(stream));
+  return e ? KNNG_E_CUDA : KNNG_OK;
+}
+
 int knng_forest(knng_ctx* c, const int8_t* codes_dev, int64_t n, int d, const int32_t* replay, int64_t n_replay,
                 int32_t* perm_dev, uint8_t* leaf_flag_dev) {
   if (!c || !codes_dev || !perm_dev || !leaf_flag_dev || (n_replay > 0 && !replay)) return KNNG_E_ARGS;
@@ -809,12 +846,12 @@ int knng_join_iter(knng_ctx* c, const int8_t* codes_dev, const uint64_t* sketch_
   cudaError_t e;
   if ((e = c->scalars.ensure(4096))) return cuda_fail(c, e, "scalar allocation");
   unsigned long long* up = c->scalars.as<unsigned long long>(256);
-  if ((e = cudaMemsetAsync(up, 0, 32, c->stream))) return cuda_fail(c, e, "update counter");
+  if ((e = cudaMemsetAsync(up, 0, 64, c->stream))) return cuda_fail(c, e, "update counter");
   const int K = c->prm.k_build;
   const int cps = c->prm.join_ctas_per_sm ? c->prm.join_ctas_per_sm : 4;
   const int cb = c->prm.join_ctas_per_sm ? c->prm.join_cblock : 4;
   if ((e = launch_join(codes_dev, sketch_dev, n, d, K, K * c->prm.rerank_mult, ids_in, scores_in, ids_out,
-                       scores_out, nullptr, up, c->num_sms, c->stream, nullptr, nullptr, cps, cb)))
+                       scores_out, nullptr, up, c->num_sms, c->stream, nullptr, nullptr, cps, cb, c->sketch_words(d))))
     return cuda_fail(c, e, "join");
   unsigned long long h = 0;
   if ((e = cudaMemcpyAsync(&h, up, 8, cudaMemcpyDeviceToHost, c->stream))) return cuda_fail(c, e, "update count");
@@ -854,8 +891,10 @@ int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on
   size_t b = size_t(n) * d + size_t(n) * (d / 64) * 8 + size_t(n) * K * 16 + size_t(T) * n * 5;
   b += std::max(f, in) + 64 * 1024;
   b += size_t(n) * q.k_eval * 8;                                   // export buffer
-  b += size_t(q.max_iterations + 1) * 64 * 8 + 4096;               // control block (per job, bounded)
+  b += size_t(q.max_iterations + 1) * 96 * 8 + 4096;               // control block (per job, bounded)
+  if (q.join_mode == KNNG_JOIN_JACOBI) b += size_t(2) * n;          // row-change flags
   if (q.join_cache && q.max_iterations > 0) b += cache_bytes(n);   // per-row candidate cache
+  if (q.sketch_mode == KNNG_SKETCH_HYPERPLANE) b += size_t(n) * 16;  // hyperplane sketches
   if (!rows_on_device) b += size_t(2) * std::min<int64_t>(kStageRows, n) * d * 4;  // host-input staging
   return int64_t(b) + (int64_t(1) << 24);                          // pool rounding slack
 }
@@ -951,6 +990,7 @@ int knng_build_batch(knng_ctx* c, knng_job* jobs, int count, knng_stats* stats) 
       S.join_candidates[it] += gs[g].join_candidates[it];
       S.join_dots[it] += gs[g].join_dots[it];
       S.join_distinct[it] += gs[g].join_distinct[it];
+      S.join_skipped[it] += gs[g].join_skipped[it];
     }
     S.join_ctas_per_sm = gs[g].join_ctas_per_sm;
     S.join_cblock = gs[g].join_cblock;

@@ -35,6 +35,10 @@
 // never falls, so with the candidate cache each row keeps its distinct ids
 // with their h and a "dot <= threshold" flag for the next iteration.
 //
+// Sketches: W 64-bit words per row, d / 64 for the reference's coordinate-sign
+// sketch or 2 for the optional 128-hyperplane sketch (hyperplane.cu); the
+// score is 1024 - popcount over the W words either way.
+//
 // Stages per row (shared memory, K = 50, R = 400, d = 1024: ~54 KB):
 //   A  own list, sketch, code row; clear table and histogram; start copying
 //      the row's cache entries into shared memory (cp.async); insert the
@@ -99,7 +103,7 @@ __host__ __device__ inline JoinSmem join_smem(int K, int R, int d) {
   s.R = R;
   s.KK = K * K;
   s.d = d;
-  s.W = d / 64;
+  s.W = d / 64;  // room for the widest sketch (the sign sketch); a hyperplane sketch uses 2 words
   s.HT = 1024;
   while (s.HT < (3 * (s.KK + K)) / 2) s.HT <<= 1;  // load factor <= 2/3
   size_t o = 0;
@@ -175,7 +179,7 @@ __device__ __forceinline__ int table_find(const int32_t* key, uint32_t mask, int
 
 template <int CB, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
-    const int8_t* __restrict__ codes, const uint64_t* __restrict__ sketch, int64_t n, int d, int K, int R,
+    const int8_t* __restrict__ codes, const uint64_t* __restrict__ sketch, int64_t n, int d, int K, int R, int W,
     const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out, int32_t* scores_out,
     const int32_t* __restrict__ row_order, unsigned long long* __restrict__ counters, JobTable jt, JoinCtl ctl) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -200,11 +204,16 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   __shared__ int32_t s_wsum[kWarps], s_wsum2[kWarps];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, sub = lane & 7, slot8 = lane >> 3;
-  const int KK = L.KK, W = L.W, nchunk = d / 16, sk_chunks = W / 2;
+  const int KK = L.KK, nchunk = d / 16, sk_chunks = W / 2;  // W: sketch words per row (<= L.W = d / 64)
   const uint32_t mask = uint32_t(L.HT - 1);
   const bool inplace = ids_out == ids_in;
   const bool cached = ctl.cache_ids != nullptr;
-  unsigned long long my_updates = 0, my_cands = 0, my_dots = 0, my_distinct = 0;
+  // per-CTA statistics, kept by thread 0 in shared memory (no registers held
+  // across the row loop): updates, sketches scored, rows reranked, distinct
+  // candidates, rows skipped
+  __shared__ unsigned long long s_stat[5];
+  if (tid == 0)
+    for (int q = 0; q < 5; ++q) s_stat[q] = 0;
   int run_job = -1;                 // per-job update count kept by warp 0 lane 0
   unsigned long long run_upd = 0;
 
@@ -233,12 +242,18 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       }
     }
     // ---- A
+    // (unchanged-row skip, double-buffered iterations only) a row whose own
+    // list and every neighbour's list came out of the previous iteration
+    // unchanged sees exactly the inputs it saw then, so its result is its
+    // current list: it is copied through without any work
+    int moved = ctl.chg_in ? 0 : 1;
     for (int k = tid; k < K; k += kThreads) {
-      pool_id[k] = ids_in[i * K + k];
+      const int32_t id = ids_in[i * K + k];
+      pool_id[k] = id;
       pool_sc[k] = scores_in[i * K + k];
+      if (ctl.chg_in) moved |= (id < 0 || id >= n) ? 1 : int(ctl.chg_in[id]);
     }
-    for (int c = tid; c < nchunk; c += kThreads) my_code[c] = reinterpret_cast<const uint4*>(codes + i * d)[c];
-    for (int c = tid; c < sk_chunks; c += kThreads) my_sk[c] = reinterpret_cast<const uint4*>(sketch + i * W)[c];
+    if (ctl.chg_in && tid == 0) moved |= int(ctl.chg_in[i]);
     if (!cached)
       for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;
     for (int t = tid; t < L.HT / 4; t += kThreads) {
@@ -252,7 +267,19 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       s_nprom = 0;
       s_ccnt = cached ? ctl.cache_cnt[i] : 0;
     }
-    __syncthreads();
+    if (__syncthreads_or(moved) == 0) {  // block-uniform
+      for (int k = tid; k < K; k += kThreads) {  // from global memory: the shared copies may be reused at once
+        ids_out[i * K + k] = ids_in[i * K + k];
+        scores_out[i * K + k] = scores_in[i * K + k];
+      }
+      if (tid == 0) {
+        ctl.chg_out[i] = 0;
+        ++s_stat[4];
+      }
+      continue;
+    }
+    for (int c = tid; c < nchunk; c += kThreads) my_code[c] = reinterpret_cast<const uint4*>(codes + i * d)[c];
+    for (int c = tid; c < sk_chunks; c += kThreads) my_sk[c] = reinterpret_cast<const uint4*>(sketch + i * W)[c];
     if (cached) {
       // stage the row's cache entries into shared memory (ids over the region
       // of stages F-H, scores over the histogram) while stage B runs; the
@@ -390,8 +417,10 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     }
     __syncthreads();
     const int cnt = s_cnt;
-    my_cands += unsigned(ncl);
-    my_distinct += unsigned(nu);
+    if (tid == 0) {
+      s_stat[1] += unsigned(ncl);
+      s_stat[3] += unsigned(nu);
+    }
     if (cnt > R) {
       // bins from h = 1024 down: thread t sums bins 4t..4t+3 (index x = 1024 - h);
       // bin x = 1024 (h = 0) is handled last
@@ -483,7 +512,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     // ---- F2  dots (8 lanes per candidate, up to eight 16-byte loads in flight per lane)
     {
       const int nneed = s_nneed;
-      my_dots += unsigned(nneed);
+      if (tid == 0) s_stat[2] += unsigned(nneed);
       const int32_t thr0 = pool_sc[K - 1];
       const int per_lane = d / 128;
       for (int wbase = warp * 4; wbase < nneed; wbase += kGroups) {
@@ -662,7 +691,8 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
         }
       }
       for (int o = 16; o > 0; o >>= 1) changed += __shfl_xor_sync(full, changed, o);
-      my_updates += unsigned(changed);
+      if (lane == 0) s_stat[0] += unsigned(changed);
+      if (ctl.chg_out && lane == 0) ctl.chg_out[i] = changed ? 1 : 0;
       if (ctl.job_upd && lane == 0) {
         if (job != run_job) {
           if (run_job >= 0 && run_upd) atomicAdd(ctl.job_upd + run_job, run_upd);
@@ -675,10 +705,11 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     __syncthreads();
   }
   if (tid == 0) {
-    atomicAdd(counters + 0, my_updates);
-    atomicAdd(counters + 1, my_cands);
-    atomicAdd(counters + 2, my_dots);
-    atomicAdd(counters + 3, my_distinct);
+    atomicAdd(counters + 0, s_stat[0]);
+    atomicAdd(counters + 1, s_stat[1]);
+    atomicAdd(counters + 2, s_stat[2]);
+    atomicAdd(counters + 3, s_stat[3]);
+    if (ctl.chg_in) atomicAdd(counters + 4, s_stat[4]);
     if (ctl.job_upd && run_job >= 0 && run_upd) atomicAdd(ctl.job_upd + run_job, run_upd);
   }
 }
@@ -797,7 +828,7 @@ cudaError_t launch_stop_check(const JobTable& jt, const JoinCtl& ctl, int K, int
 cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, int d, int K, int R,
                         const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out, int32_t* scores_out,
                         const int32_t* row_order, unsigned long long* counters, int num_sms, cudaStream_t s,
-                        const JobTable* jt, const JoinCtl* ctl, int ctas_per_sm, int cblock) {
+                        const JobTable* jt, const JoinCtl* ctl, int ctas_per_sm, int cblock, int sk_words) {
   const size_t smem = join_smem(K, R, d).bytes;
   const JobTable no_jobs{};
   const JoinCtl no_ctl{};
@@ -809,8 +840,9 @@ cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, 
     }
     const int64_t blocks = std::min<int64_t>(n, int64_t(num_sms) * max_per_sm);
     cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
-    kern<<<unsigned(blocks), kThreads, smem, s>>>(codes, sketch, n, d, K, R, ids_in, scores_in, ids_out, scores_out,
-                                                  row_order, counters, jt ? *jt : no_jobs, ctl ? *ctl : no_ctl);
+    kern<<<unsigned(blocks), kThreads, smem, s>>>(codes, sketch, n, d, K, R, sk_words > 0 ? sk_words : d / 64, ids_in,
+                                                  scores_in, ids_out, scores_out, row_order, counters,
+                                                  jt ? *jt : no_jobs, ctl ? *ctl : no_ctl);
     e = cudaGetLastError();
   };
   // ctas_per_sm 3: up to 85 registers per thread (no spills), 3 resident CTAs;

@@ -55,6 +55,11 @@ __device__ __forceinline__ int job_of(const JobTable& jt, int64_t row) {
 cudaError_t launch_quantize(const float* x, int64_t n, int d, int quant_mode, int8_t* codes,
                             uint64_t* sketch, cudaStream_t s);
 
+// ---- hyperplane.cu ----
+// 128-bit sketches [n][2] of the int8 codes from 128 seeded integer hyperplanes.
+cudaError_t launch_hyperplane_sketch(const int8_t* codes, int64_t n, int d, uint32_t seed, uint64_t* sketch,
+                                     int num_sms, cudaStream_t s);
+
 // ---- scan.cu ----
 // Exclusive prefix sum of n int32 values into out (out may alias in); total
 // (device int64, may be null) receives the sum.  tmp must hold
@@ -120,7 +125,8 @@ cudaError_t launch_init_block(const int8_t* codes, int d, int64_t n_total, int K
 // ---- join.cu ----
 // Per-batch NN-Descent control block in device memory.
 struct JoinCtl {
-  unsigned long long* counters;   // [4]: updates, sketches scored, reranked rows, distinct candidates
+  unsigned long long* counters;   // [5]: updates, sketches scored, reranked rows, distinct candidates,
+                                  // rows skipped as unchanged
   unsigned long long* job_upd;    // [count]: updates of this iteration per job
   int* job_done;                  // [count]: job stopped (its rows pass through)
   float* job_prev;                // [count]: previous iteration's update rate
@@ -137,6 +143,11 @@ struct JoinCtl {
   int* cache_cnt;                 // [n]: entries held (0 before the first iteration)
   int cache_cap;
   int64_t row_limit;              // rows processed (the first ones in visit order); 0: all
+  // Unchanged-row skip of double-buffered iterations (both null: none).
+  // chg_in[i] = 1 when row i's list changed in the previous iteration (all 1
+  // before the first); the launch writes this iteration's flags to chg_out.
+  const uint8_t* chg_in;
+  uint8_t* chg_out;
 };
 // Entries per row of the candidate cache (rows with more distinct candidates
 // keep the first ones; the rest are scored again) and its bytes for n rows.
@@ -149,7 +160,8 @@ cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, 
                         const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out,
                         int32_t* scores_out, const int32_t* row_order, unsigned long long* counters,
                         int num_sms, cudaStream_t s, const JobTable* jt = nullptr,
-                        const JoinCtl* ctl = nullptr, int ctas_per_sm = 0, int cblock = 4);
+                        const JoinCtl* ctl = nullptr, int ctas_per_sm = 0, int cblock = 4, int sk_words = 0);
+// sk_words: 64-bit sketch words per row (0: d / 64, the sign sketch; 2: hyperplane sketch)
 // ctas_per_sm: 4 (64 registers per thread) or 3 (up to 85, no spills);
 // cblock: sketch candidates in flight per 8-lane group in the Hamming stage
 // (2, 4 or 8).  Both are chosen by the autotuner.

@@ -53,6 +53,29 @@ def all_knn(x, k=32, block=2048, margin=64):
     return ids, sc
 
 
+def sample_knn(x, rows, k=15, block=500, margin=64):
+    """Exact top-k neighbours, self excluded, of the given rows of x (torch CUDA
+    float32 [n, d]) by float64 inner product: a float32 pass keeps the best
+    k + margin candidates, which are rescored in float64 and ordered by (score
+    desc, candidate position).  Returns 0-based ids as numpy int64 [len(rows), k]."""
+    import torch
+
+    rows = torch.as_tensor(np.asarray(rows), device=x.device)
+    m = min(x.shape[0] - 1, k + margin)
+    out = []
+    for s in range(0, len(rows), block):
+        q = rows[s:s + block]
+        sims = x[q] @ x.T
+        sims[torch.arange(len(q), device=x.device), q] = -float("inf")
+        cand = sims.topk(m, dim=1).indices
+        del sims
+        exact = torch.einsum("bd,bmd->bm", x[q].double(), x[cand].double())
+        exact[cand == q[:, None]] = -float("inf")
+        order = exact.argsort(dim=1, descending=True, stable=True)[:, :k]
+        out.append(torch.gather(cand, 1, order).cpu())
+    return torch.cat(out).numpy()
+
+
 def recall(gt_knns_1based, pred_knns_1based):
     """evaluate_submission.py:17-26: per row, the first k gt ids other than the
     row itself, intersected with the row's predicted ids."""

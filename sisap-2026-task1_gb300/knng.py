@@ -22,6 +22,7 @@ JOIN_JACOBI, JOIN_INPLACE = 0, 1
 ORDER_NATURAL, ORDER_LEAF = 0, 1
 GRAM_DP4A, GRAM_TCGEN05 = 0, 1
 INIT_FOREST, INIT_RANDOM, INIT_BLOCK = 0, 1, 2
+SKETCH_SIGN, SKETCH_HYPERPLANE = 0, 1
 
 STATUS = {0: "ok", -1: "E_ARGS", -2: "E_DIM", -3: "E_OOM", -4: "E_ADMIT", -5: "E_TIMEOUT", -6: "E_CUDA",
           -7: "E_REPLAY", -8: "E_BUSY", -9: "E_NOTFOUND", -10: "E_SCRATCH"}
@@ -41,7 +42,7 @@ class Params(C.Structure):
         ("row_order", C.c_int), ("seed", C.c_uint32), ("device", C.c_int), ("autotune", C.c_int),
         ("use_graph", C.c_int), ("gram_mode", C.c_int), ("init_mode", C.c_int), ("join_cache", C.c_int),
         ("block_size", C.c_int), ("bridges", C.c_int), ("wait_limit", C.c_int), ("join_ctas_per_sm", C.c_int),
-        ("join_cblock", C.c_int),
+        ("join_cblock", C.c_int), ("sketch_mode", C.c_int),
     ]
 
 
@@ -53,10 +54,11 @@ class Stats(C.Structure):
         ("device_s", C.c_double), ("join_ms", C.c_double * 64), ("join_candidates", C.c_int64 * 64),
         ("join_dots", C.c_int64 * 64), ("kernel_launches", C.c_int64), ("join_ctas_per_sm", C.c_int),
         ("join_cblock", C.c_int), ("graph_used", C.c_int), ("join_distinct", C.c_int64 * 64),
+        ("join_skipped", C.c_int64 * 64),
     ]
 
     def as_dict(self):
-        arrays = ("updates", "join_ms", "join_candidates", "join_dots", "join_distinct")
+        arrays = ("updates", "join_ms", "join_candidates", "join_dots", "join_distinct", "join_skipped")
         d = {f: getattr(self, f) for f, _ in self._fields_ if f not in arrays}
         for f in arrays:
             d[f] = list(getattr(self, f)[: self.iterations])
@@ -67,7 +69,7 @@ EXPORTS = ["knng_default_params", "knng_create", "knng_destroy", "knng_build", "
            "knng_last_error", "knng_quantize", "knng_forest", "knng_init_graph", "knng_join_iter", "knng_export",
            "knng_init_graph_noalloc", "knng_footprint_bytes", "knng_trim", "knng_server_default_params",
            "knng_server_create", "knng_submit", "knng_poll", "knng_wait", "knng_release", "knng_server_destroy",
-           "knng_pca"]
+           "knng_pca", "knng_sketch_hyperplane"]
 
 _lib = None
 
@@ -92,6 +94,7 @@ def lib():
         L.knng_last_error.argtypes = [V]
         L.knng_last_error.restype = C.c_char_p
         L.knng_quantize.argtypes = [V, I64, C.c_int, C.c_int, V, V, V]
+        L.knng_sketch_hyperplane.argtypes = [V, I64, C.c_int, C.c_uint32, V, V]
         L.knng_forest.argtypes = [V, V, I64, C.c_int, V, I64, V, V]
         L.knng_init_graph.argtypes = [V, V, I64, C.c_int, V, V, V, V]
         L.knng_join_iter.argtypes = [V, V, V, I64, C.c_int, V, V, V, V, P(I64)]
@@ -377,6 +380,21 @@ def quantize(x, quant_mode=QUANT_TRUNC, stream=None):
         raise KnngError(st, "knng_quantize")
     torch.cuda.synchronize(x.device)
     return codes, sk
+
+
+def sketch_hyperplane(codes, seed=1337, stream=None):
+    """Optional 128-bit hyperplane sketches of int8 codes (CUDA tensor (n, d)):
+    returns int64 (n, 2) holding the two 64-bit words of each row."""
+    import torch
+
+    n, d = codes.shape
+    sk = torch.empty((n, 2), dtype=torch.int64, device=codes.device)
+    _ready(codes)
+    st = lib().knng_sketch_hyperplane(_ptr(codes), n, d, seed, _ptr(sk), _stream_ptr(stream))
+    if st != 0:
+        raise KnngError(st, "knng_sketch_hyperplane")
+    torch.cuda.synchronize(codes.device)
+    return sk
 
 
 def pca(x, dims, device=0):

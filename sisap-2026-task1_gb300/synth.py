@@ -60,6 +60,28 @@ def mixture_torch(n: int, d: int, centres: int, seed: int, device="cuda", chunk:
     return out
 
 
+def subspace(n: int, d: int, m: int, seed: int, chunk: int = 65536) -> np.ndarray:
+    """(n, d) float32 unit rows spread over a random m-dimensional subspace.
+
+    x = normalise(z A) with z ~ N(0, I_m) per row and one Gaussian m x d basis
+    A: data of low intrinsic dimension, like embeddings whose spectrum decays
+    fast.  Here the int8 codes keep the neighbour order well enough that the
+    reference algorithm reaches recall@15 in the reference's published range
+    (m = 64, 100k rows: about 84 % in 7 iterations), so recall differences of
+    half a point are measurable -- unlike the isotropic mixture, where every
+    method sits near 30-45 %.  float64 numpy with PCG64, cast to float32.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = rng.standard_normal((m, d))
+    out = np.empty((n, d), dtype=np.float32)
+    for s in range(0, n, chunk):
+        e = min(n, s + chunk)
+        x = rng.standard_normal((e - s, m)) @ a
+        x /= np.sqrt(np.sum(x * x, axis=1, keepdims=True))
+        out[s:e] = x
+    return out
+
+
 def exact_knn(x: np.ndarray, k: int, rows=None, block: int = 2048) -> np.ndarray:
     """Exact top-k neighbours (0-based ids, self excluded) by float64 inner product.
 

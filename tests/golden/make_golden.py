@@ -7,7 +7,7 @@ input.  The inputs themselves are not stored: the file keeps the generator
 arguments and the SHA-256 of the float32 bytes, and the tests regenerate them.
 
 Run from the repository root after `make -C oracle all ref`:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [NAME ...]      # all fixtures, or the named ones
 """
 from __future__ import annotations
 
@@ -24,7 +24,7 @@ sys.path.insert(0, os.path.join(ROOT, "sisap-2026-task1_gb300"))
 import oracle as O  # noqa: E402
 import synth  # noqa: E402
 
-# name: (kind, n, d, centres, seed)
+# name: (kind, n, d, centres or subspace dimension, seed)
 CASES = {
     "mix_n2000_d1024": ("mixture", 2000, 1024, 20, 11),
     "mix_n3000_d384": ("mixture", 3000, 384, 30, 12),
@@ -33,6 +33,9 @@ CASES = {
     "edge_n300_d1024": ("edge", 300, 1024, 3, 15),
     "tiny_n40_d1024": ("mixture", 40, 1024, 4, 16),
     "tiny_n2_d1024": ("mixture", 2, 1024, 1, 17),
+    # low intrinsic dimension (synth.subspace): the reference reaches high recall
+    "sub_n8000_d1024_m32": ("subspace", 8000, 1024, 32, 18),
+    "sub_n6000_d768_m48": ("subspace", 6000, 768, 48, 19),
 }
 
 # Values at the quantiser's corners (src/main.cpp:184-190): sub-code positives
@@ -46,6 +49,8 @@ EDGE_VALUES = np.array([0.5 / 127, -0.5 / 127, 1.0, -1.0, 1.02, -1.5, 127.4 / 12
 
 
 def make_input(kind, n, d, centres, seed):
+    if kind == "subspace":
+        return synth.subspace(n, d, centres, seed)
     x = synth.mixture(n, d, centres, seed)
     if kind == "edge":
         rng = np.random.Generator(np.random.PCG64(seed + 1))
@@ -59,8 +64,10 @@ def digest(x):
     return hashlib.sha256(np.ascontiguousarray(x, dtype=np.float32).tobytes()).hexdigest()
 
 
-def main():
+def main(names=None):
     for name, (kind, n, d, c, seed) in CASES.items():
+        if names and name not in names:
+            continue
         x = make_input(kind, n, d, c, seed)
         knns, dists, attrs, out = O.run_reference(x, threads=1)
         iters = sum(1 for ln in out.splitlines() if "-> Iteration" in ln)
@@ -71,4 +78,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -56,7 +56,8 @@ def _check_export(x, knns, dists):
         assert len(np.unique(row)) == len(row)
 
 
-@pytest.mark.parametrize("name", ["mix_n2000_d1024", "mix_n6000_d1024_c600", "mix_n3000_d384", "mix_n2500_d768"])
+@pytest.mark.parametrize("name", ["mix_n2000_d1024", "mix_n6000_d1024_c600", "mix_n3000_d384", "mix_n2500_d768",
+                                  "sub_n8000_d1024_m32", "sub_n6000_d768_m48"])
 @pytest.mark.parametrize("join", ["jacobi", "inplace"])
 def test_build_recall_vs_reference(knng_mod, name, join):
     knng = knng_mod
@@ -188,7 +189,9 @@ def test_build_one_million_properties(knng_mod):
     sims[torch.arange(len(rows)), torch.from_numpy(rows).cuda()] = -np.inf
     gt = sims.topk(15, dim=1).indices.cpu().numpy()
     rec = synth.recall_at_k(kh, gt, rows=rows)
-    assert rec > 0.3, rec  # sanity floor; reference-relative recall is checked on the fixtures
+    # sanity floor only: recall relative to the reference algorithm on these
+    # same rows is tests/test_gpu_parity_scale.py
+    assert rec > 0.3, rec
 
 
 def test_build_degenerate_duplicates(knng_mod):

@@ -10,6 +10,9 @@ double-buffered, stable-tie restatement of src/main.cpp:320-440:
 * whole builds with the candidate cache on, from the GPU's own initial graph
   (itself bit-exact against the oracle on the same forest) through the
   reference's early stop (src/main.cpp:432-439) to the exported knns/dists.
+  These builds also copy unchanged rows through (a row whose list and
+  neighbours' lists did not change in the previous iteration); the oracle
+  computes every row, so the comparison covers that skip too.
 """
 import os
 
@@ -120,6 +123,9 @@ def test_build_variant_with_cache_bit_exact(env, build_case, ctas, cblock):
     assert st.join_ctas_per_sm == ctas and st.join_cblock == cblock
     assert st.iterations == it_ref
     assert list(st.updates[: st.iterations]) == ups_ref
+    # rows whose inputs did not change are copied through from the third iteration on
+    assert st.join_skipped[0] == 0 and st.join_skipped[1] == 0
+    assert sum(st.join_skipped[: st.iterations]) > 0
     np.testing.assert_array_equal(k, k_ref)
     np.testing.assert_array_equal(dd, d_ref)
 
