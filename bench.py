@@ -573,6 +573,12 @@ def run_gpu(args):
                        "l2": "inputs (n x d float32) far larger than L2; no flush",
                        "parallelism": f"replicas x{ws}"},
             "build_s": last.build_s, "step_s": last.device_s, "iterations": it,
+            "join_iterations": {"ms": [round(last.join_ms[i], 3) for i in range(it)],
+                                "updates": [int(last.updates[i]) for i in range(it)],
+                                "rows_skipped_unchanged": [int(last.join_skipped[i]) for i in range(it)],
+                                "distinct_candidates": [int(last.join_distinct[i]) for i in range(it)],
+                                "sketches_scored": [int(last.join_candidates[i]) for i in range(it)],
+                                "rows_reranked": [int(last.join_dots[i]) for i in range(it)]},
             "stage_s": {"quantize": last.quantize_s, "forest": last.forest_s, "init": last.init_s,
                         "join": last.join_s, "export": last.export_s},
             "recall@15": rec, "recall_rows": args.recall_rows, "recall_parity_100k": parity,

@@ -83,7 +83,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
-  __shared__ int s_abort;
   unsigned char* stage[2] = {smem, smem + kStageBytes};
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -97,7 +96,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    s_abort = 0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -108,8 +106,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
   uint32_t phase[2] = {0, 0};
   int pending[2] = {0, 0};  // commits issued on a stage and not yet waited for
   const int64_t npairs = (nleaves + 1) / 2;
+  // Aborting is decided only from __syncthreads_or over every thread's wait
+  // outcome, so every thread takes the same path to the drain (a flag in
+  // shared memory written by one thread and read by another without a barrier
+  // in between would split the block across different barriers).
+  bool aborted = false;
 
-  for (int64_t pr = blockIdx.x; pr < npairs && !s_abort; pr += gridDim.x) {
+  for (int64_t pr = blockIdx.x; pr < npairs && !aborted; pr += gridDim.x) {
     int64_t ls[2], lm[2];
     for (int h = 0; h < 2; ++h) {
       const int64_t l = 2 * pr + h;
@@ -127,17 +130,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
     const int8_t* src = live_row ? codes + int64_t(perm[ls[hrow] + mrow]) * d : nullptr;
     for (int c = 0; c < nchunks; ++c) {
       const int st = c & 1;
+      int gave_up = 0;
       if (pending[st]) {  // the MMAs that read this stage two chunks ago must be done
         if (mbar_wait(smem_u32(&mbar[st]), phase[st], spin_limit)) {
           phase[st] ^= 1;
           pending[st] = 0;
-        } else {  // gave up: pending stays set, so the drain below still waits for this commit
-          if (tid == 0) atomicOr(err, kErrTimeout);
-          s_abort = 1;
+        } else {
+          gave_up = 1;  // pending stays set, so the drain below still waits for this commit
         }
       }
-      __syncthreads();
-      if (s_abort) break;  // block-uniform: s_abort is read after the barrier
+      if (__syncthreads_or(gave_up)) {
+        aborted = true;
+        break;
+      }
       // row tid, 128 codes -> 16 core-matrix rows of 8 bf16 (16 bytes each)
       unsigned char* base = stage[st] + (tid >> 3) * 2048 + (tid & 7) * 16;
 #pragma unroll
@@ -177,18 +182,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
       }
       pending[st] = 1;
     }
-    if (s_abort) break;
+    if (aborted) break;
     // the last commit covers every MMA of this tile
     const int last = (nchunks - 1) & 1;
+    int gave_up = 0;
     if (mbar_wait(smem_u32(&mbar[last]), phase[last], spin_limit)) {
       phase[last] ^= 1;
       pending[last] = 0;
     } else {
-      if (tid == 0) atomicOr(err, kErrTimeout);
-      s_abort = 1;
+      gave_up = 1;
     }
-    __syncthreads();
-    if (s_abort) break;  // block-uniform, as above
+    if (__syncthreads_or(gave_up)) {
+      aborted = true;
+      break;
+    }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     // warp w reads TMEM lanes 32w..32w+31 = rows of X; warps 0-1 hold leaf 0
     // (columns 0-63), warps 2-3 leaf 1 (columns 64-127)
@@ -217,6 +224,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
   // drain: wait for any commit still outstanding (thread 0 issued them and
   // knows which), always with the full limit, so tensor memory is never freed
   // under an MMA in flight; then free it
+  if (aborted && tid == 0) atomicOr(err, kErrTimeout);
   if (tid == 0)
     for (int st = 0; st < 2; ++st)
       if (pending[st]) mbar_wait(smem_u32(&mbar[st]), phase[st], kSpinLimit);

@@ -334,7 +334,11 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
           if (n2 >= 0 && n2 < n && n2 != i) sl = table_insert(key, mask, n2, 0u);
           cand_slot[j] = int16_t(sl);
           if (sl >= 0) {
-            first = atomicMin(&meta[sl], uint32_t(j)) == kFirstMask;
+            // rounds visit j in increasing order, so once a slot records a
+            // smaller first j (a plain read suffices) this occurrence is not
+            // the first; otherwise the atomic decides, and exactly one of the
+            // threads that saw the slot untouched gets kFirstMask back
+            if (meta[sl] > uint32_t(j)) first = atomicMin(&meta[sl], uint32_t(j)) == kFirstMask;
             ++local_cnt;
           }
         }
@@ -498,14 +502,24 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     // ---- F1  selected distinct ids that are not starting-list members need a dot
     {
       const int ht = s_ht, jcut = ht >= 0 ? s_jcut : 0;
-      for (int q = tid; q < nu; q += kThreads) {
-        const int sl = ulist[q];
-        const uint32_t m = meta[sl];
-        const int h = int((m >> 16) & 0x7ffu);
-        const bool sel = ht < 0 || h > ht || (h == ht && int(m & kFirstMask) <= jcut);
-        // a cached rejection stands: the row's threshold never falls, so a
-        // dot once <= it stays <= it
-        if (sel && !(uint32_t(key[sl]) & kPoolFlag) && !(m & kRej)) need[atomicAdd(&s_nneed, 1)] = int16_t(sl);
+      for (int q0 = warp * 32; q0 < nu; q0 += kThreads) {  // warp-uniform trip count
+        const int q = q0 + lane;
+        bool want = false;
+        int sl = -1;
+        if (q < nu) {
+          sl = ulist[q];
+          const uint32_t m = meta[sl];
+          const int h = int((m >> 16) & 0x7ffu);
+          const bool sel = ht < 0 || h > ht || (h == ht && int(m & kFirstMask) <= jcut);
+          // a cached rejection stands: the row's threshold never falls, so a
+          // dot once <= it stays <= it
+          want = sel && !(uint32_t(key[sl]) & kPoolFlag) && !(m & kRej);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, want);
+        int base = 0;
+        if (lane == 0 && bal) base = atomicAdd(&s_nneed, __popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (want) need[base + __popc(bal & ((1u << lane) - 1u))] = int16_t(sl);
       }
     }
     __syncthreads();
