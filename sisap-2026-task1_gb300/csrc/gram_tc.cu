@@ -10,18 +10,27 @@
 //
 // Tile: two leaves (<= 64 members each) stacked as one 128-row operand X;
 // one MMA chain computes D = X * X^T (M = N = 128) and the two 64 x 64
-// diagonal blocks are the two leaves' Gram blocks.  X is staged 128 columns of
-// d at a time into one of two shared-memory stages in the K-major core-matrix
-// layout (8 rows x 16 bytes per core matrix, no swizzle; LBO = 128 B between
-// core matrices along K, SBO = 2048 B between 8-row groups), converting int8
-// to bf16 on the way (TMA cannot convert).  One thread issues 8 MMAs (K = 16
-// each) per stage and commits them to the stage's mbarrier; the stage is
-// refilled only after that barrier flips.  D lives in 128 TMEM columns; warp w
-// reads lanes 32w..32w+31 with tcgen05.ld.  Every mbarrier wait is bounded (the
-// limit is a launch argument): on timeout the kernel records kErrTimeout, the
-// whole block stops issuing work at the next barrier, thread 0 waits with the
-// full limit for every MMA it committed and the tensor memory is freed before
-// the kernel returns.
+// diagonal blocks are the two leaves' Gram blocks.  X moves through a
+// software pipeline of 64-column steps (d/64 per tile, continuing across the
+// CTA's tiles):
+//   * cp.async copies step g + 3's int8 chunk (128 rows x 64 bytes, gathered
+//     through the leaf permutation) into a 4-slot ring, so the loads of three
+//     steps are in flight while step g is converted and multiplied;
+//   * 256 threads widen step g's int8 chunk to bf16 (exact: |q| <= 128)
+//     in shared memory, into the K-major core-matrix layout the MMA reads
+//     (8 rows x 16 bytes per core matrix, no swizzle; LBO = 128 B between
+//     core matrices along K, SBO = 1024 B between 8-row groups), in one of two
+//     bf16 stages (TMA cannot convert);
+//   * one thread issues the step's 4 MMAs (K = 16 each) and commits them to
+//     the stage's mbarrier; a stage is rewritten only after its barrier flips.
+// At a tile's last step D (128 TMEM columns) is read with tcgen05.ld: warps w
+// and w + 4 share lane quadrant w % 4 and read half of its leaf's 64 columns
+// each.  Three CTAs per SM (65 KB of shared memory, 128 TMEM columns each).
+// Every mbarrier wait is bounded (the limit is a launch argument).  Giving up
+// is decided by __syncthreads_or over every thread's wait outcome, so the
+// whole block leaves together; the kernel then records kErrTimeout, waits for
+// its copies, lets thread 0 wait with the full limit for every MMA it
+// committed, and frees its tensor memory before returning.
 #include "knng_internal.cuh"
 
 #include <algorithm>
@@ -29,9 +38,15 @@
 namespace knng {
 namespace {
 
-constexpr int kTcThreads = 128;
-constexpr int kChunk = 128;                     // d columns per stage
-constexpr int kStageBytes = 128 * kChunk * 2;   // 128 rows x 128 bf16 = 32 KB
+constexpr int kTcThreads = 256;
+constexpr int kCtasPerSm = 3;
+constexpr int kChunk = 64;                      // d columns per pipeline step
+constexpr int kRing = 4;                        // int8 ring slots: copies issued 3 steps ahead
+constexpr int kAhead = kRing - 1;
+constexpr int kRowBufs = 4;                     // tiles whose row ids are resident
+constexpr int kI8Bytes = 128 * kChunk;          // 8 KB: a step's 128 rows of int8
+constexpr int kStageBytes = 128 * kChunk * 2;   // 16 KB: the same rows widened to bf16
+constexpr int kSbo = (kChunk / 8) * 128;        // 1024 B between 8-row groups of a stage
 constexpr uint32_t kTmemCols = 128;
 constexpr long long kSpinLimit = 1ll << 26;
 
@@ -67,23 +82,36 @@ __host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
 }
 
-__device__ __forceinline__ uint32_t bf16x2(int a, int b) {
-  // int8 values widened exactly: bf16 of a float integer in [-128, 127]
-  const uint32_t lo = __float_as_uint(float(a)) >> 16;
-  const uint32_t hi = __float_as_uint(float(b)) >> 16;
-  return lo | (hi << 16);
+// Two int8 values widened to a bf16 pair (lo in the low half): exact, every
+// integer in [-128, 127] has at most 8 significant bits.
+__device__ __forceinline__ uint32_t bf16x2(int lo, int hi) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(float(hi)), "f"(float(lo)));
+  return r;
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __restrict__ codes, int d,
-                                                             const int32_t* __restrict__ perm,
-                                                             const int32_t* __restrict__ leaf_start,
-                                                             int64_t nleaves, int64_t total,
-                                                             int32_t* __restrict__ gram, unsigned* err,
-                                                             long long spin_limit) {
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int8_t* __restrict__ codes, int d,
+                                                                      const int32_t* __restrict__ perm,
+                                                                      const int32_t* __restrict__ leaf_start,
+                                                                      int64_t nleaves, int64_t total,
+                                                                      int32_t* __restrict__ gram, unsigned* err,
+                                                                      long long spin_limit) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
+  __shared__ int32_t row_id[kRowBufs][128];            // id of X's row r in a tile, -1 past a leaf's end
+  __shared__ int32_t tile_ls[kRowBufs][2], tile_lm[kRowBufs][2];  // start and size of the tile's two leaves
   unsigned char* stage[2] = {smem, smem + kStageBytes};
+  unsigned char* ring = smem + 2 * kStageBytes;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (warp == 0) {
@@ -97,137 +125,173 @@ __global__ void __launch_bounds__(kTcThreads, 1) leaf_gram_tc(const int8_t* __re
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  const int nchunks = d / kChunk;
+  const int64_t npairs = (nleaves + 1) / 2;
+  const int64_t ntiles = int64_t(blockIdx.x) < npairs ? (npairs - 1 - int64_t(blockIdx.x)) / gridDim.x + 1 : 0;
+  const int64_t nsteps = ntiles * nchunks;
+
+  // tile q of this CTA is the leaf pair blockIdx.x + q * gridDim.x; its row
+  // ids and leaf extents go to row buffer q % kRowBufs
+  auto fill_rows = [&](int64_t q) {
+    if (q >= ntiles || tid >= 128) return;
+    const int64_t pr = int64_t(blockIdx.x) + q * gridDim.x;
+    const int b = int(q % kRowBufs), h = tid >> 6, m = tid & 63;
+    const int64_t l = 2 * pr + h;
+    int64_t s0 = 0, len = 0;
+    if (l < nleaves) {
+      s0 = leaf_start[l];
+      len = (l + 1 < nleaves ? leaf_start[l + 1] : total) - s0;
+    }
+    row_id[b][tid] = m < len ? perm[s0 + m] : -1;
+    if (m == 0) {
+      tile_ls[b][h] = int32_t(s0);
+      tile_lm[b][h] = int32_t(len);
+    }
+  };
+  // step g's copies (int8 chunk c of tile q) into ring slot g % kRing: one
+  // commit group per step, empty past the last step
+  auto issue = [&](int64_t g) {
+    if (g < nsteps) {
+      const int64_t q = g / nchunks;
+      const int c = int(g - q * nchunks);
+      const int b = int(q % kRowBufs);
+      unsigned char* dst = ring + (g % kRing) * kI8Bytes;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int idx = tid + kTcThreads * u;  // 512 pieces of 16 bytes: row idx / 4, piece idx % 4
+        const int r = idx >> 2, pc = idx & 3;
+        const int32_t id = row_id[b][r];
+        if (id >= 0) cp_async16(dst + r * kChunk + pc * 16, codes + int64_t(id) * d + c * kChunk + pc * 16);
+      }
+    }
+    cp_async_commit();
+  };
+
+  for (int q = 0; q < kRowBufs; ++q) fill_rows(q);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t taddr = tmem_base;
   const uint32_t idesc = instr_desc(128, 128);
-  const int nchunks = d / kChunk;
   uint32_t phase[2] = {0, 0};
-  int pending[2] = {0, 0};  // commits issued on a stage and not yet waited for
-  const int64_t npairs = (nleaves + 1) / 2;
-  // Aborting is decided only from __syncthreads_or over every thread's wait
-  // outcome, so every thread takes the same path to the drain (a flag in
-  // shared memory written by one thread and read by another without a barrier
-  // in between would split the block across different barriers).
-  bool aborted = false;
+  int pending[2] = {0, 0};  // commits issued on a stage and not yet waited for (thread 0's view counts)
+  bool aborted = false;     // block-uniform: set only from __syncthreads_or
+  for (int g = 0; g < kAhead; ++g) issue(g);
 
-  for (int64_t pr = blockIdx.x; pr < npairs && !aborted; pr += gridDim.x) {
-    int64_t ls[2], lm[2];
-    for (int h = 0; h < 2; ++h) {
-      const int64_t l = 2 * pr + h;
-      if (l < nleaves) {
-        ls[h] = leaf_start[l];
-        lm[h] = (l + 1 < nleaves ? leaf_start[l + 1] : total) - ls[h];
+  for (int64_t g = 0; g < nsteps; ++g) {
+    const int64_t q = g / nchunks;
+    const int c = int(g - q * nchunks);
+    const int st = int(g & 1);
+    const int b = int(q % kRowBufs);
+    // the buffer of tile q - 1, whose epilogue ended at the last barrier; its
+    // new tile's first copies are issued at least 3 steps from now
+    if (c == 0 && q >= 1) fill_rows(q + kRowBufs - 1);
+    issue(g + kAhead);  // into the slot of step g - 1, converted before the last barrier
+    cp_async_wait<kAhead>();  // this thread's copies of step g have landed
+    int gave_up = 0;
+    if (pending[st]) {  // the MMAs of step g - 2 read this stage
+      if (mbar_wait(smem_u32(&mbar[st]), phase[st], spin_limit)) {
+        phase[st] ^= 1;
+        pending[st] = 0;
       } else {
-        ls[h] = 0;
-        lm[h] = 0;
+        gave_up = 1;  // pending stays set: the drain waits for that commit
       }
     }
-    // this thread stages row r = tid of X: leaf tid/64, member tid%64
-    const int hrow = tid >> 6, mrow = tid & 63;
-    const bool live_row = mrow < lm[hrow];
-    const int8_t* src = live_row ? codes + int64_t(perm[ls[hrow] + mrow]) * d : nullptr;
-    for (int c = 0; c < nchunks; ++c) {
-      const int st = c & 1;
-      int gave_up = 0;
-      if (pending[st]) {  // the MMAs that read this stage two chunks ago must be done
-        if (mbar_wait(smem_u32(&mbar[st]), phase[st], spin_limit)) {
-          phase[st] ^= 1;
-          pending[st] = 0;
-        } else {
-          gave_up = 1;  // pending stays set, so the drain below still waits for this commit
+    if (__syncthreads_or(gave_up)) {  // also publishes every thread's copies of step g
+      aborted = true;
+      break;
+    }
+    {  // thread t widens 32 codes of X's row t / 2 into the core-matrix layout
+      const int r = tid >> 1, half = tid & 1;
+      const bool live = row_id[b][r] >= 0;
+      const unsigned char* src = ring + (g % kRing) * kI8Bytes + r * kChunk + half * 32;
+      unsigned char* dst = stage[st] + (r >> 3) * kSbo + (r & 7) * 16 + half * 4 * 128;
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const uint4 v = live ? *reinterpret_cast<const uint4*>(src + 16 * p) : make_uint4(0, 0, 0, 0);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const uint32_t a = w[2 * e], bb = w[2 * e + 1];
+          uint4 o;
+          o.x = bf16x2(int(int8_t(a)), int(int8_t(a >> 8)));
+          o.y = bf16x2(int(int8_t(a >> 16)), int(int8_t(a >> 24)));
+          o.z = bf16x2(int(int8_t(bb)), int(int8_t(bb >> 8)));
+          o.w = bf16x2(int(int8_t(bb >> 16)), int(int8_t(bb >> 24)));
+          *reinterpret_cast<uint4*>(dst + (2 * p + e) * 128) = o;
         }
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = smem_u32(stage[st]);
+#pragma unroll
+      for (int kk = 0; kk < kChunk / 16; ++kk) {
+        const uint64_t desc = smem_desc(sa + kk * 256, 128, kSbo);
+        const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+            "l"(desc), "l"(desc), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&mbar[st]))
+                   : "memory");
+    }
+    pending[st] = 1;
+    if (c == nchunks - 1) {  // the tile's last step: its commit covers every MMA of the tile
+      gave_up = 0;
+      if (mbar_wait(smem_u32(&mbar[st]), phase[st], spin_limit)) {
+        phase[st] ^= 1;
+        pending[st] = 0;
+      } else {
+        gave_up = 1;
       }
       if (__syncthreads_or(gave_up)) {
         aborted = true;
         break;
       }
-      // row tid, 128 codes -> 16 core-matrix rows of 8 bf16 (16 bytes each)
-      unsigned char* base = stage[st] + (tid >> 3) * 2048 + (tid & 7) * 16;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of X: leaf h = (w % 4) / 2,
+      // member (w % 2) * 32 + lane; warps w < 4 take the leaf's first 32 columns
+      const int quad = warp & 3, h = quad >> 1, mi = (quad & 1) * 32 + lane, j0 = 32 * (warp >> 2);
+      const int lm = tile_lm[b][h];
+      int32_t* out = mi < lm ? gram + (int64_t(tile_ls[b][h]) + mi) * int64_t(kMaxLeaf) : nullptr;
+      const uint32_t lane_addr = taddr + (uint32_t(quad * 32) << 16) + uint32_t(64 * h + j0);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        int4 v = make_int4(0, 0, 0, 0);
-        if (live_row) v = __ldg(reinterpret_cast<const int4*>(src + c * kChunk) + q);
-        const int w[4] = {v.x, v.y, v.z, v.w};
+      for (int hq = 0; hq < 2; ++hq) {
+        uint32_t rr[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]),
+              "=r"(rr[7]), "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]),
+              "=r"(rr[14]), "=r"(rr[15])
+            : "r"(lane_addr + hq * 16)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (out) {
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          uint4 o;
-          const int a = w[2 * h], b = w[2 * h + 1];
-          o.x = bf16x2(int(int8_t(a)), int(int8_t(a >> 8)));
-          o.y = bf16x2(int(int8_t(a >> 16)), int(int8_t(a >> 24)));
-          o.z = bf16x2(int(int8_t(b)), int(int8_t(b >> 8)));
-          o.w = bf16x2(int(int8_t(b >> 16)), int(int8_t(b >> 24)));
-          *reinterpret_cast<uint4*>(base + (2 * q + h) * 128) = o;
+          for (int j = 0; j < 16; ++j) {
+            const int jj = j0 + 16 * hq + j;
+            if (jj < lm) out[jj] = __float2int_rn(__uint_as_float(rr[j]));
+          }
         }
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t sa = smem_u32(stage[st]);
-#pragma unroll
-        for (int kk = 0; kk < kChunk / 16; ++kk) {
-          const uint64_t desc = smem_desc(sa + kk * 256, 128, 2048);
-          const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
-              "l"(desc), "l"(desc), "r"(idesc), "r"(acc)
-              : "memory");
-        }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         smem_u32(&mbar[st]))
-                     : "memory");
-      }
-      pending[st] = 1;
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();  // D is read before the next tile's first MMA overwrites it
     }
-    if (aborted) break;
-    // the last commit covers every MMA of this tile
-    const int last = (nchunks - 1) & 1;
-    int gave_up = 0;
-    if (mbar_wait(smem_u32(&mbar[last]), phase[last], spin_limit)) {
-      phase[last] ^= 1;
-      pending[last] = 0;
-    } else {
-      gave_up = 1;
-    }
-    if (__syncthreads_or(gave_up)) {
-      aborted = true;
-      break;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    // warp w reads TMEM lanes 32w..32w+31 = rows of X; warps 0-1 hold leaf 0
-    // (columns 0-63), warps 2-3 leaf 1 (columns 64-127)
-    const int h = warp >> 1, mi = (warp & 1) * 32 + lane;
-    const uint32_t lane_addr = taddr + (uint32_t(warp * 32) << 16) + uint32_t(h * 64);
-    int32_t* out = (mi < lm[h]) ? gram + (ls[h] + mi) * int64_t(kMaxLeaf) : nullptr;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      uint32_t r[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-          : "r"(lane_addr + q * 16)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (out) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j)
-          if (q * 16 + j < lm[h]) out[q * 16 + j] = __float2int_rn(__uint_as_float(r[j]));
-      }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // D is read before the next tile's first MMA overwrites it
   }
-  // drain: wait for any commit still outstanding (thread 0 issued them and
-  // knows which), always with the full limit, so tensor memory is never freed
-  // under an MMA in flight; then free it
+  // drain: no copy may land after the exit, every committed MMA must be done
+  // before the tensor memory is freed (thread 0 issued them and knows which;
+  // always the full limit), then free it
+  cp_async_wait<0>();
   if (aborted && tid == 0) atomicOr(err, kErrTimeout);
   if (tid == 0)
-    for (int st = 0; st < 2; ++st)
-      if (pending[st]) mbar_wait(smem_u32(&mbar[st]), phase[st], kSpinLimit);
+    for (int s2 = 0; s2 < 2; ++s2)
+      if (pending[s2]) mbar_wait(smem_u32(&mbar[s2]), phase[s2], kSpinLimit);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -241,11 +305,11 @@ cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm,
                                 int64_t nleaves, int64_t total, int32_t* gram, unsigned* err, int num_sms,
                                 cudaStream_t s, int wait_limit) {
   if (d % kChunk != 0) return cudaErrorInvalidValue;
-  const size_t smem = 2 * size_t(kStageBytes) + 1024;
+  const size_t smem = 2 * size_t(kStageBytes) + size_t(kRing) * kI8Bytes + 1024;  // + alignment slack
   KNNG_CUDA_TRY(ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram_tc), smem));
   const int64_t pairs = (nleaves + 1) / 2;
-  // two CTAs per SM at most: 2 x 128 TMEM columns of the 512, and ~65 KB shared memory each
-  const int64_t blocks = std::min<int64_t>(pairs, int64_t(num_sms) * 2);
+  // three CTAs per SM: 3 x 128 TMEM columns of the 512, ~67 KB of shared memory each
+  const int64_t blocks = std::min<int64_t>(pairs, int64_t(num_sms) * kCtasPerSm);
   if (blocks <= 0) return cudaSuccess;
   cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   // wait_limit > 0: polls per wait; 0: the default; < 0: every wait in the
