@@ -547,7 +547,8 @@ def run_gpu(args):
     # ---- recall on a seeded sample
     rec = recall_sample(x, knns, rows=args.recall_rows) if args.recall_rows > 0 and rank == 0 else None
     # ---- the same build on the reference arm's own sample rows (like-for-like N)
-    same = same_sample_gpu(dev, args.steps, max(1, args.warmup)) if rank == 0 and ws == 1 else None
+    # (part of the CPU-baseline leg: --skip-cpu leaves both out)
+    same = same_sample_gpu(dev, args.steps, max(1, args.warmup)) if rank == 0 and ws == 1 and not args.skip_cpu else None
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     parity = None

@@ -1,10 +1,10 @@
 // gram_tc.cu -- K3 on the 5th-generation tensor cores: leaf Gram blocks with
-// tcgen05.mma (bf16 operands, fp32 accumulation in tensor memory).
+// tcgen05.mma (f16 operands, fp32 accumulation in tensor memory).
 //
 // Reference: the dots of src/main.cpp:261-269 (every pair of members of a
 // leaf).  ptxas rejects tcgen05.mma.kind::i8 for sm_103a, so the int8 codes are
-// widened to bf16 (exact: |q| <= 128 needs 8 significant bits) and multiplied
-// with kind::f16 into fp32 accumulators.  Every partial sum is an integer of
+// widened to f16 (exact: every integer in [-128, 127] is an f16) and
+// multiplied with kind::f16 into fp32 accumulators.  Every partial sum is an integer of
 // magnitude <= d * 128 * 128 <= 2^24, which fp32 represents exactly, so the
 // result equals the int32 dot bit for bit (checked against the dp4a kernel).
 //
@@ -16,16 +16,19 @@
 //   * cp.async copies step g + 3's int8 chunk (128 rows x 64 bytes, gathered
 //     through the leaf permutation) into a 4-slot ring, so the loads of three
 //     steps are in flight while step g is converted and multiplied;
-//   * 256 threads widen step g's int8 chunk to bf16 (exact: |q| <= 128)
-//     in shared memory, into the K-major core-matrix layout the MMA reads
-//     (8 rows x 16 bytes per core matrix, no swizzle; LBO = 128 B between
-//     core matrices along K, SBO = 1024 B between 8-row groups), in one of two
-//     bf16 stages (TMA cannot convert);
+//   * 256 threads widen step g's int8 chunk to f16 in shared memory (two
+//     integer ops and one packed half add per four codes), into the K-major
+//     core-matrix layout the MMA reads (8 rows x 16 bytes per core matrix, no
+//     swizzle; LBO = 128 B between core matrices along K, SBO = 1024 B between
+//     8-row groups), in one of two f16 stages (TMA cannot convert);
 //   * one thread issues the step's 4 MMAs (K = 16 each) and commits them to
 //     the stage's mbarrier; a stage is rewritten only after its barrier flips.
 // At a tile's last step D (128 TMEM columns) is read with tcgen05.ld: warps w
 // and w + 4 share lane quadrant w % 4 and read half of its leaf's 64 columns
 // each.  Three CTAs per SM (65 KB of shared memory, 128 TMEM columns each).
+// Each thread waits for the next step's copies before the step's single
+// barrier, so one barrier per step publishes both the f16 stage the MMAs
+// read and the int8 chunk the next step widens.
 // Every mbarrier wait is bounded (the limit is a launch argument).  Giving up
 // is decided by __syncthreads_or over every thread's wait outcome, so the
 // whole block leaves together; the kernel then records kErrTimeout, waits for
@@ -45,7 +48,7 @@ constexpr int kRing = 4;                        // int8 ring slots: copies issue
 constexpr int kAhead = kRing - 1;
 constexpr int kRowBufs = 4;                     // tiles whose row ids are resident
 constexpr int kI8Bytes = 128 * kChunk;          // 8 KB: a step's 128 rows of int8
-constexpr int kStageBytes = 128 * kChunk * 2;   // 16 KB: the same rows widened to bf16
+constexpr int kStageBytes = 128 * kChunk * 2;   // 16 KB: the same rows widened to f16
 constexpr int kSbo = (kChunk / 8) * 128;        // 1024 B between 8-row groups of a stage
 constexpr uint32_t kTmemCols = 128;
 constexpr long long kSpinLimit = 1ll << 26;
@@ -77,17 +80,21 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;
 }
 
-// Instruction descriptor, kind::f16: D f32, A and B bf16, both K-major, N, M.
+// Instruction descriptor, kind::f16: D f32, A and B f16 (type 0), both K-major, N, M.
 __host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+  return (1u << 4) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
 }
 
-// Two int8 values widened to a bf16 pair (lo in the low half): exact, every
-// integer in [-128, 127] has at most 8 significant bits.
-__device__ __forceinline__ uint32_t bf16x2(int lo, int hi) {
-  uint32_t r;
-  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(float(hi)), "f"(float(lo)));
-  return r;
+// Four int8 codes (one 32-bit word) widened to two f16 pairs, exactly and in
+// integer/packed-half steps: u = code + 128 (xor 0x80 per byte) becomes the f16
+// 1024 + u by placing 0x64 above each byte (0x6400 is 1024.0, whose unit in the
+// last place is 1), and one packed add of -1152 leaves code = u - 128.
+__device__ __forceinline__ void widen4(uint32_t w, uint32_t& lo, uint32_t& hi) {
+  const uint32_t u = w ^ 0x80808080u;
+  const uint32_t a = __byte_perm(u, 0x64646464u, 0x4140);  // codes 0, 1
+  const uint32_t b = __byte_perm(u, 0x64646464u, 0x4342);  // codes 2, 3
+  asm("add.f16x2 %0, %1, %2;" : "=r"(lo) : "r"(a), "r"(0xE480E480u));
+  asm("add.f16x2 %0, %1, %2;" : "=r"(hi) : "r"(b), "r"(0xE480E480u));
 }
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
@@ -127,15 +134,14 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
   }
   const int nchunks = d / kChunk;
   const int64_t npairs = (nleaves + 1) / 2;
-  const int64_t ntiles = int64_t(blockIdx.x) < npairs ? (npairs - 1 - int64_t(blockIdx.x)) / gridDim.x + 1 : 0;
-  const int64_t nsteps = ntiles * nchunks;
+  const int ntiles = int64_t(blockIdx.x) < npairs ? int((npairs - 1 - int64_t(blockIdx.x)) / gridDim.x) + 1 : 0;
 
   // tile q of this CTA is the leaf pair blockIdx.x + q * gridDim.x; its row
   // ids and leaf extents go to row buffer q % kRowBufs
-  auto fill_rows = [&](int64_t q) {
+  auto fill_rows = [&](int q) {
     if (q >= ntiles || tid >= 128) return;
-    const int64_t pr = int64_t(blockIdx.x) + q * gridDim.x;
-    const int b = int(q % kRowBufs), h = tid >> 6, m = tid & 63;
+    const int64_t pr = int64_t(blockIdx.x) + int64_t(q) * gridDim.x;
+    const int b = q & (kRowBufs - 1), h = tid >> 6, m = tid & 63;
     const int64_t l = 2 * pr + h;
     int64_t s0 = 0, len = 0;
     if (l < nleaves) {
@@ -148,23 +154,28 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
       tile_lm[b][h] = int32_t(len);
     }
   };
-  // step g's copies (int8 chunk c of tile q) into ring slot g % kRing: one
-  // commit group per step, empty past the last step
-  auto issue = [&](int64_t g) {
-    if (g < nsteps) {
-      const int64_t q = g / nchunks;
-      const int c = int(g - q * nchunks);
-      const int b = int(q % kRowBufs);
-      unsigned char* dst = ring + (g % kRing) * kI8Bytes;
+  // The copy stream runs kAhead steps ahead of the compute: (iq, ic) is the
+  // tile and chunk of the next step to copy, islot its ring slot.  One commit
+  // group per step, empty past the last tile.
+  int iq = 0, ic = 0, islot = 0;
+  auto issue_next = [&]() {
+    if (iq < ntiles) {
+      const int b = iq & (kRowBufs - 1);
+      unsigned char* dst = ring + islot * kI8Bytes;
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
         const int idx = tid + kTcThreads * u;  // 512 pieces of 16 bytes: row idx / 4, piece idx % 4
         const int r = idx >> 2, pc = idx & 3;
         const int32_t id = row_id[b][r];
-        if (id >= 0) cp_async16(dst + r * kChunk + pc * 16, codes + int64_t(id) * d + c * kChunk + pc * 16);
+        if (id >= 0) cp_async16(dst + r * kChunk + pc * 16, codes + int64_t(id) * d + ic * kChunk + pc * 16);
+      }
+      if (++ic == nchunks) {
+        ic = 0;
+        ++iq;
       }
     }
     cp_async_commit();
+    islot = (islot + 1) & (kRing - 1);
   };
 
   for (int q = 0; q < kRowBufs; ++q) fill_rows(q);
@@ -176,20 +187,22 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
   uint32_t phase[2] = {0, 0};
   int pending[2] = {0, 0};  // commits issued on a stage and not yet waited for (thread 0's view counts)
   bool aborted = false;     // block-uniform: set only from __syncthreads_or
-  for (int g = 0; g < kAhead; ++g) issue(g);
+  for (int g = 0; g < kAhead; ++g) issue_next();
+  cp_async_wait<kAhead - 1>();  // the first step's copies
+  __syncthreads();
 
-  for (int64_t g = 0; g < nsteps; ++g) {
-    const int64_t q = g / nchunks;
-    const int c = int(g - q * nchunks);
-    const int st = int(g & 1);
-    const int b = int(q % kRowBufs);
-    // the buffer of tile q - 1, whose epilogue ended at the last barrier; its
-    // new tile's first copies are issued at least 3 steps from now
+  // Invariant at the top of a step: its int8 chunk is in ring slot `slot`,
+  // visible to every thread.  One barrier per step: each thread waits for
+  // the next step's copies before it, so the barrier publishes both this
+  // step's f16 stage and the next step's int8 chunk.
+  int q = 0, c = 0, st = 0, slot = 0;
+  while (q < ntiles) {
+    const int b = q & (kRowBufs - 1);
+    // the buffer of tile q - 1, whose epilogue ended at a barrier; its new
+    // tile's first copies are issued at least one barrier from now
     if (c == 0 && q >= 1) fill_rows(q + kRowBufs - 1);
-    issue(g + kAhead);  // into the slot of step g - 1, converted before the last barrier
-    cp_async_wait<kAhead>();  // this thread's copies of step g have landed
     int gave_up = 0;
-    if (pending[st]) {  // the MMAs of step g - 2 read this stage
+    if (pending[st]) {  // the MMAs of two steps ago read this stage
       if (mbar_wait(smem_u32(&mbar[st]), phase[st], spin_limit)) {
         phase[st] ^= 1;
         pending[st] = 0;
@@ -197,33 +210,30 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
         gave_up = 1;  // pending stays set: the drain waits for that commit
       }
     }
-    if (__syncthreads_or(gave_up)) {  // also publishes every thread's copies of step g
-      aborted = true;
-      break;
-    }
-    {  // thread t widens 32 codes of X's row t / 2 into the core-matrix layout
+    if (!gave_up) {  // thread t widens 32 codes of X's row t / 2 into the core-matrix layout
       const int r = tid >> 1, half = tid & 1;
       const bool live = row_id[b][r] >= 0;
-      const unsigned char* src = ring + (g % kRing) * kI8Bytes + r * kChunk + half * 32;
+      const unsigned char* src = ring + slot * kI8Bytes + r * kChunk + half * 32;
       unsigned char* dst = stage[st] + (r >> 3) * kSbo + (r & 7) * 16 + half * 4 * 128;
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
         const uint4 v = live ? *reinterpret_cast<const uint4*>(src + 16 * p) : make_uint4(0, 0, 0, 0);
-        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          const uint32_t a = w[2 * e], bb = w[2 * e + 1];
-          uint4 o;
-          o.x = bf16x2(int(int8_t(a)), int(int8_t(a >> 8)));
-          o.y = bf16x2(int(int8_t(a >> 16)), int(int8_t(a >> 24)));
-          o.z = bf16x2(int(int8_t(bb)), int(int8_t(bb >> 8)));
-          o.w = bf16x2(int(int8_t(bb >> 16)), int(int8_t(bb >> 24)));
-          *reinterpret_cast<uint4*>(dst + (2 * p + e) * 128) = o;
-        }
+        uint4 o0, o1;
+        widen4(v.x, o0.x, o0.y);
+        widen4(v.y, o0.z, o0.w);
+        widen4(v.z, o1.x, o1.y);
+        widen4(v.w, o1.z, o1.w);
+        *reinterpret_cast<uint4*>(dst + (2 * p) * 128) = o0;
+        *reinterpret_cast<uint4*>(dst + (2 * p + 1) * 128) = o1;
       }
     }
+    issue_next();               // into the slot of the previous step, converted before the last barrier
+    cp_async_wait<kAhead - 1>();  // this thread's copies of the next step have landed
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
+    if (__syncthreads_or(gave_up)) {
+      aborted = true;
+      break;
+    }
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t sa = smem_u32(stage[st]);
@@ -282,6 +292,12 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();  // D is read before the next tile's first MMA overwrites it
+    }
+    st ^= 1;
+    slot = (slot + 1) & (kRing - 1);
+    if (++c == nchunks) {
+      c = 0;
+      ++q;
     }
   }
   // drain: no copy may land after the exit, every committed MMA must be done
