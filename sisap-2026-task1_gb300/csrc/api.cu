@@ -213,7 +213,7 @@ int ensure_scratch(knng_ctx* c, int64_t n, Scratch* s, int64_t n_replay) {
   {
     char* p = c->scratch.as<char>();
     InitBufs& b = s->ib;
-    b.gram = reinterpret_cast<int32_t*>(p); carve(p, tn * kMaxLeaf * 4);
+    b.gram = reinterpret_cast<int32_t*>(p); carve(p, size_t(init_gram_trees(T)) * size_t(n) * kMaxLeaf * 4);
     b.pos = reinterpret_cast<int32_t*>(p); carve(p, tn * 4);
     b.leaf_lo = reinterpret_cast<int32_t*>(p); carve(p, tn * 4);
     b.leaf_idx = reinterpret_cast<int32_t*>(p); carve(p, tn * 8);
@@ -463,8 +463,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   ctl.all_done = c->jobs.as<int>(o_flags);
   ctl.final_buf = c->jobs.as<int>(o_flags) + 1;
   ctl.upd_log = c->jobs.as<long long>(o_log);
-  ctl.cache_ids = nullptr;
-  ctl.cache_hr = nullptr;
+  ctl.cache_ent = nullptr;
   ctl.cache_cnt = nullptr;
   ctl.cache_cap = 0;
   ctl.row_limit = 0;  // every row
@@ -472,13 +471,13 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   ctl.chg_out = nullptr;
   const bool skip_rows = p.join_mode == KNNG_JOIN_JACOBI && MI > 0;
   if (skip_rows && (e = c->rowflags.ensure(size_t(2) * size_t(N)))) return cuda_fail(c, e, "row flag allocation");
-  if (p.join_cache && MI > 0) {
+  int64_t max_job = 0;
+  for (int b = 0; b < J; ++b) max_job = std::max<int64_t>(max_job, hn[b]);
+  if (p.join_cache && MI > 0 && max_job < kCacheMaxJobRows) {
     if ((e = c->cache.ensure(cache_bytes(N)))) return cuda_fail(c, e, "candidate cache allocation");
     char* cp = c->cache.as<char>();
-    ctl.cache_ids = reinterpret_cast<int32_t*>(cp);
+    ctl.cache_ent = reinterpret_cast<uint32_t*>(cp);
     cp += (size_t(N) * kCacheCap * 4 + 255) & ~size_t(255);
-    ctl.cache_hr = reinterpret_cast<uint16_t*>(cp);
-    cp += (size_t(N) * kCacheCap * 2 + 255) & ~size_t(255);
     ctl.cache_cnt = reinterpret_cast<int*>(cp);
     ctl.cache_cap = kCacheCap;
   }
@@ -524,11 +523,10 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   // rows in tree-0 leaf order (no forest with the random or block init: natural order)
   const int32_t* order = (p.row_order == KNNG_ORDER_LEAF && forest_init) ? c->perm.as<int32_t>() : nullptr;
   JoinCtl tune_ctl{};  // the candidate cache alone, for the second autotune sweep
-  tune_ctl.cache_ids = ctl.cache_ids;
-  tune_ctl.cache_hr = ctl.cache_hr;
+  tune_ctl.cache_ent = ctl.cache_ent;
   tune_ctl.cache_cnt = ctl.cache_cnt;
   tune_ctl.cache_cap = ctl.cache_cap;
-  const JoinCfg cfg = autotune_join(c, N, d, ids, scs, order, tune_counters, ctl.cache_ids ? &tune_ctl : nullptr);
+  const JoinCfg cfg = autotune_join(c, N, d, ids, scs, order, tune_counters, ctl.cache_ent ? &tune_ctl : nullptr);
   cudaEventRecord(c->ev[3], str);
   // every row starts the phase with an empty candidate cache, and counts as
   // changed before the first iteration
@@ -543,7 +541,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   const char* step = "";
   if (p.use_graph) {
     const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->join_sketch()), uintptr_t(c->graph.p),
-                                        uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(ctl.cache_ids),
+                                        uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(ctl.cache_ent),
                                         uintptr_t(c->rowflags.p),
                                         uintptr_t(N), uintptr_t(d),
                                         uintptr_t(J), uintptr_t(o), uintptr_t(cfg.early.first), uintptr_t(cfg.early.second),
@@ -893,7 +891,7 @@ int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on
   b += size_t(n) * q.k_eval * 8;                                   // export buffer
   b += size_t(q.max_iterations + 1) * 96 * 8 + 4096;               // control block (per job, bounded)
   if (q.join_mode == KNNG_JOIN_JACOBI) b += size_t(2) * n;          // row-change flags
-  if (q.join_cache && q.max_iterations > 0) b += cache_bytes(n);   // per-row candidate cache
+  if (q.join_cache && q.max_iterations > 0 && n < kCacheMaxJobRows) b += cache_bytes(n);  // candidate cache
   if (q.sketch_mode == KNNG_SKETCH_HYPERPLANE) b += size_t(n) * 16;  // hyperplane sketches
   if (!rows_on_device) b += size_t(2) * std::min<int64_t>(kStageRows, n) * d * 4;  // host-input staging
   return int64_t(b) + (int64_t(1) << 24);                          // pool rounding slack

@@ -46,7 +46,7 @@ constexpr int kCtasPerSm = 3;
 constexpr int kChunk = 64;                      // d columns per pipeline step
 constexpr int kRing = 4;                        // int8 ring slots: copies issued 3 steps ahead
 constexpr int kAhead = kRing - 1;
-constexpr int kRowBufs = 4;                     // tiles whose row ids are resident
+constexpr int kRowBufs = 8;                     // tiles whose row ids are resident (refilled 7 tiles ahead)
 constexpr int kI8Bytes = 128 * kChunk;          // 8 KB: a step's 128 rows of int8
 constexpr int kStageBytes = 128 * kChunk * 2;   // 16 KB: the same rows widened to f16
 constexpr int kSbo = (kChunk / 8) * 128;        // 1024 B between 8-row groups of a stage
@@ -100,6 +100,9 @@ __device__ __forceinline__ void widen4(uint32_t w, uint32_t& lo, uint32_t& hi) {
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -110,8 +113,8 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
                                                                       const int32_t* __restrict__ perm,
                                                                       const int32_t* __restrict__ leaf_start,
                                                                       int64_t nleaves, int64_t total,
-                                                                      int32_t* __restrict__ gram, unsigned* err,
-                                                                      long long spin_limit) {
+                                                                      int32_t* __restrict__ gram, int64_t gram_pos0,
+                                                                      unsigned* err, long long spin_limit) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
@@ -137,18 +140,29 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
   const int ntiles = int64_t(blockIdx.x) < npairs ? int((npairs - 1 - int64_t(blockIdx.x)) / gridDim.x) + 1 : 0;
 
   // tile q of this CTA is the leaf pair blockIdx.x + q * gridDim.x; its row
-  // ids and leaf extents go to row buffer q % kRowBufs
-  auto fill_rows = [&](int q) {
+  // ids and leaf extents go to row buffer q % kRowBufs.  Thread t < 128
+  // handles X's row t: leaf h = t / 64, member m = t % 64.
+  auto leaf_extent = [&](int q, int64_t& s0, int64_t& len) {
+    s0 = 0;
+    len = 0;
     if (q >= ntiles || tid >= 128) return;
-    const int64_t pr = int64_t(blockIdx.x) + int64_t(q) * gridDim.x;
-    const int b = q & (kRowBufs - 1), h = tid >> 6, m = tid & 63;
-    const int64_t l = 2 * pr + h;
-    int64_t s0 = 0, len = 0;
+    const int64_t l = 2 * (int64_t(blockIdx.x) + int64_t(q) * gridDim.x) + (tid >> 6);
     if (l < nleaves) {
       s0 = leaf_start[l];
       len = (l + 1 < nleaves ? leaf_start[l + 1] : total) - s0;
     }
-    row_id[b][tid] = m < len ? perm[s0 + m] : -1;
+  };
+  // the row id arrives by cp.async (in the caller's next commit group) or,
+  // for the initial tiles, by a plain load
+  auto fill_rows = [&](int q, int64_t s0, int64_t len, bool async) {
+    if (q >= ntiles || tid >= 128) return;
+    const int b = q & (kRowBufs - 1), h = tid >> 6, m = tid & 63;
+    if (m < len) {
+      if (async) cp_async4(&row_id[b][tid], perm + s0 + m);
+      else row_id[b][tid] = perm[s0 + m];
+    } else {
+      row_id[b][tid] = -1;
+    }
     if (m == 0) {
       tile_ls[b][h] = int32_t(s0);
       tile_lm[b][h] = int32_t(len);
@@ -178,7 +192,11 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
     islot = (islot + 1) & (kRing - 1);
   };
 
-  for (int q = 0; q < kRowBufs; ++q) fill_rows(q);
+  for (int q = 0; q < kRowBufs; ++q) {
+    int64_t s0, len;
+    leaf_extent(q, s0, len);
+    fill_rows(q, s0, len, false);
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -196,11 +214,16 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
   // the next step's copies before it, so the barrier publishes both this
   // step's f16 stage and the next step's int8 chunk.
   int q = 0, c = 0, st = 0, slot = 0;
+  int64_t f_s0 = 0, f_len = 0;  // extent of the tile being refilled, loaded one step ahead
   while (q < ntiles) {
     const int b = q & (kRowBufs - 1);
-    // the buffer of tile q - 1, whose epilogue ended at a barrier; its new
-    // tile's first copies are issued at least one barrier from now
-    if (c == 0 && q >= 1) fill_rows(q + kRowBufs - 1);
+    // Tile q + 7 reuses the buffer of tile q - 1, whose epilogue ended at a
+    // barrier: its leaf extent is loaded at the tile's first step (used a
+    // step later, so the load does not stall the barrier) and its row ids
+    // are copied at the second step, in that step's commit group, which is
+    // waited for a dozen steps before the first copy that reads them.
+    if (q >= 1 && c == 0) leaf_extent(q + kRowBufs - 1, f_s0, f_len);
+    if (q >= 1 && c == 1) fill_rows(q + kRowBufs - 1, f_s0, f_len, true);
     int gave_up = 0;
     if (pending[st]) {  // the MMAs of two steps ago read this stage
       if (mbar_wait(smem_u32(&mbar[st]), phase[st], spin_limit)) {
@@ -269,7 +292,7 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
       // member (w % 2) * 32 + lane; warps w < 4 take the leaf's first 32 columns
       const int quad = warp & 3, h = quad >> 1, mi = (quad & 1) * 32 + lane, j0 = 32 * (warp >> 2);
       const int lm = tile_lm[b][h];
-      int32_t* out = mi < lm ? gram + (int64_t(tile_ls[b][h]) + mi) * int64_t(kMaxLeaf) : nullptr;
+      int32_t* out = mi < lm ? gram + (int64_t(tile_ls[b][h]) - gram_pos0 + mi) * int64_t(kMaxLeaf) : nullptr;
       const uint32_t lane_addr = taddr + (uint32_t(quad * 32) << 16) + uint32_t(64 * h + j0);
 #pragma unroll
       for (int hq = 0; hq < 2; ++hq) {
@@ -318,8 +341,8 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
 }  // namespace
 
 cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm, const int32_t* leaf_start,
-                                int64_t nleaves, int64_t total, int32_t* gram, unsigned* err, int num_sms,
-                                cudaStream_t s, int wait_limit) {
+                                int64_t nleaves, int64_t total, int32_t* gram, int64_t gram_pos0, unsigned* err,
+                                int num_sms, cudaStream_t s, int wait_limit) {
   if (d % kChunk != 0) return cudaErrorInvalidValue;
   const size_t smem = 2 * size_t(kStageBytes) + size_t(kRing) * kI8Bytes + 1024;  // + alignment slack
   KNNG_CUDA_TRY(ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram_tc), smem));
@@ -331,8 +354,8 @@ cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm,
   // wait_limit > 0: polls per wait; 0: the default; < 0: every wait in the
   // main loop gives up at once (the drain keeps the full limit)
   const long long spins = wait_limit > 0 ? (long long)wait_limit : wait_limit < 0 ? 0ll : kSpinLimit;
-  leaf_gram_tc<<<unsigned(blocks), kTcThreads, smem, s>>>(codes, d, perm, leaf_start, nleaves, total, gram, err,
-                                                          spins);
+  leaf_gram_tc<<<unsigned(blocks), kTcThreads, smem, s>>>(codes, d, perm, leaf_start, nleaves, total, gram, gram_pos0,
+                                                          err, spins);
   note_launch();
   return cudaGetLastError();
 }

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(kGramThreads) leaf_gram(const int8_t* __restri
                                                           const int32_t* __restrict__ perm,
                                                           const int32_t* __restrict__ leaf_start,
                                                           int64_t nleaves, int64_t total,
-                                                          int32_t* __restrict__ gram) {
+                                                          int32_t* __restrict__ gram, int64_t gram_pos0) {
   extern __shared__ uint4 rows_s[];
   const int stride16 = d / 16 + 1;  // in uint4
   for (int64_t l = blockIdx.x; l < nleaves; l += gridDim.x) {
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kGramThreads) leaf_gram(const int8_t* __restri
     for (int a = 0; a < 4; ++a) {
       const int r = ty * 4 + a;
       if (r >= m) break;
-      int32_t* out = gram + (s + r) * int64_t(kMaxLeaf);
+      int32_t* out = gram + (s + r - gram_pos0) * int64_t(kMaxLeaf);
 #pragma unroll
       for (int b = 0; b < 8; ++b)
         if (b < jmax) out[tx + 8 * b] = acc[a][b];
@@ -141,24 +141,40 @@ __device__ __forceinline__ uint64_t list_insert(uint64_t& kA, uint64_t& kB, uint
   return (K - 1) < 32 ? __shfl_sync(full, kA, K - 1) : __shfl_sync(full, kB, K - 33);
 }
 
-// K4: one warp per row; merge the row's T leaf Gram rows into the top-K list.
-__global__ void __launch_bounds__(256) init_merge(int64_t n, int T, int K, const int32_t* __restrict__ perm,
+// K4: one warp per row; merge the row's leaf Gram rows of trees [t0, t1) into
+// its top-K list.  The first chunk of trees starts from an empty list, later
+// chunks from the list the previous chunk wrote (keys round-trip exactly, and
+// an empty entry, id -1 / INT32_MIN, is key 0), so the chunks give the list of
+// all trees at once.  Gram rows are stored from position gram_pos0 on.
+__global__ void __launch_bounds__(256) init_merge(int64_t n, int t0, int t1, int K, int first, int last,
+                                                  const int32_t* __restrict__ perm,
                                                   const int32_t* __restrict__ pos,
                                                   const int32_t* __restrict__ leaf_lo,
                                                   const uint8_t* __restrict__ leaf_sz,
-                                                  const int32_t* __restrict__ gram, int32_t* __restrict__ ids,
-                                                  int32_t* __restrict__ scores, int32_t* __restrict__ fix_rows,
-                                                  int64_t* __restrict__ fix_count) {
+                                                  const int32_t* __restrict__ gram, int64_t gram_pos0,
+                                                  int32_t* __restrict__ ids, int32_t* __restrict__ scores,
+                                                  int32_t* __restrict__ fix_rows, int64_t* __restrict__ fix_count) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
   for (int64_t i = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
     uint64_t kA = 0, kB = 0, thr = 0;
-    for (int t = 0; t < T; ++t) {
+    if (!first) {
+      if (lane < K) {
+        const int32_t id = ids[i * K + lane];
+        kA = id >= 0 ? make_key(scores[i * K + lane], id) : 0;
+      }
+      if (32 + lane < K) {
+        const int32_t id = ids[i * K + 32 + lane];
+        kB = id >= 0 ? make_key(scores[i * K + 32 + lane], id) : 0;
+      }
+      thr = (K - 1) < 32 ? __shfl_sync(0xffffffffu, kA, K - 1) : __shfl_sync(0xffffffffu, kB, K - 33);
+    }
+    for (int t = t0; t < t1; ++t) {
       const int64_t p = pos[int64_t(t) * n + i];
       const int64_t s = leaf_lo[p];
       const int m = leaf_sz[p];
       const int self = int(p - s);
-      const int32_t* grow = gram + p * int64_t(kMaxLeaf);
+      const int32_t* grow = gram + (p - gram_pos0) * int64_t(kMaxLeaf);
 #pragma unroll
       for (int half = 0; half < 2; ++half) {
         const int j = lane + 32 * half;
@@ -184,7 +200,7 @@ __global__ void __launch_bounds__(256) init_merge(int64_t n, int T, int K, const
       gi[32 + lane] = kB ? key_id(kB) : -1;
       gs[32 + lane] = kB ? key_score(kB) : kScoreMinI;
     }
-    if (real < K && lane == 0) {
+    if (last && real < K && lane == 0) {
       const int64_t slot = atomicAdd(reinterpret_cast<unsigned long long*>(fix_count), 1ull);
       fix_rows[slot] = int32_t(i);
     }
@@ -481,7 +497,7 @@ size_t init_bytes(int64_t n, int T, int leaf) {
   const size_t tn = size_t(T) * n;
   size_t b = tn * 4 * 3 + tn;           // pos, leaf_lo, leaf_idx, leaf_sz
   b += tn * 4;                          // leaf starts
-  b += tn * kMaxLeaf * 4;               // gram rows
+  b += size_t(init_gram_trees(T)) * n * kMaxLeaf * 4;  // gram rows of one chunk of trees
   b += size_t(n) * 4;                   // fix rows
   b += scan_tmp_bytes(int64_t(tn)) + 4096;
   return b;
@@ -510,31 +526,51 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
   leaf_starts<<<g, 256, 0, s>>>(leaf_flag, ib.leaf_idx, tn, leaf_start);
   note_launch();
   int64_t nleaves = 0;
+  // leaves before each tree's first position (the exclusive flag scan there):
+  // tree t's leaves are [lt[t], lt[t + 1])
+  int32_t lt[65] = {};  // num_trees <= 64; a fixed array: this stage allocates nothing on the host either
+  if (T > 64) return fail(cudaErrorInvalidValue, "num_trees");
   if ((e = cudaMemcpyAsync(&nleaves, ib.dev_i64, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "leaf count");
+  if ((e = cudaMemcpy2DAsync(lt, sizeof(int32_t), ib.leaf_idx, size_t(n) * sizeof(int32_t), sizeof(int32_t),
+                             size_t(T), cudaMemcpyDeviceToHost, s)))
+    return fail(e, "tree leaf offsets");
   if ((e = cudaStreamSynchronize(s))) return fail(e, "leaf table");
+  lt[T] = int32_t(nleaves);
   if (leaves_out) *leaves_out = nleaves;
   cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   leaf_fill<<<unsigned(std::min<int64_t>(grid1(nleaves), int64_t(sms) * 32)), 256, 0, s>>>(
       leaf_start, nleaves, tn, n, perm, ib.pos, ib.leaf_lo, ib.leaf_sz);
   note_launch();
   unsigned* gerr = reinterpret_cast<unsigned*>(ib.dev_i64 + 3);
-  if (gram_mode == 1) {
-    if ((e = cudaMemsetAsync(gerr, 0, sizeof(unsigned), s))) return fail(e, "gram flag");
-    if ((e = launch_leaf_gram_tc(codes, d, perm, leaf_start, nleaves, tn, ib.gram, gerr, sms, s, wait_limit)))
-      return fail(e, "tensor-core gram");
-  } else {
-    const size_t smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
-    if ((e = ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram), smem))) return fail(e, "gram smem");
+  if (gram_mode == 1 && (e = cudaMemsetAsync(gerr, 0, sizeof(unsigned), s))) return fail(e, "gram flag");
+  if ((e = cudaMemsetAsync(ib.dev_i64 + 1, 0, 8, s))) return fail(e, "fix count");
+  const size_t gram_smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
+  if (gram_mode != 1 && (e = ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram), gram_smem)))
+    return fail(e, "gram smem");
+  // kInitTreeChunk trees at a time: their leaf Gram rows (the scratch holds
+  // that many trees' worth), then the merge of those rows into the lists
+  for (int t0 = 0; t0 < T; t0 += kInitTreeChunk) {
+    const int t1 = std::min(T, t0 + kInitTreeChunk);
+    const int64_t l0 = lt[t0], l1 = lt[t1];
+    const int64_t pos0 = int64_t(t0) * n, pos1 = int64_t(t1) * n;
+    if (l1 > l0) {
+      if (gram_mode == 1) {
+        if ((e = launch_leaf_gram_tc(codes, d, perm, leaf_start + l0, l1 - l0, pos1, ib.gram, pos0, gerr, sms, s,
+                                     wait_limit)))
+          return fail(e, "tensor-core gram");
+      } else {
+        cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
+        leaf_gram<<<unsigned(std::min<int64_t>(l1 - l0, int64_t(sms) * 24)), kGramThreads, gram_smem, s>>>(
+            codes, d, perm, leaf_start + l0, l1 - l0, pos1, ib.gram, pos0);
+        note_launch();
+      }
+    }
     cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
-    leaf_gram<<<unsigned(std::min<int64_t>(nleaves, int64_t(sms) * 24)), kGramThreads, smem, s>>>(
-        codes, d, perm, leaf_start, nleaves, tn, ib.gram);
+    init_merge<<<unsigned(std::min<int64_t>((n + 7) / 8, int64_t(sms) * 16)), 256, 0, s>>>(
+        n, t0, t1, K, t0 == 0 ? 1 : 0, t1 == T ? 1 : 0, perm, ib.pos, ib.leaf_lo, ib.leaf_sz, ib.gram, pos0, ids,
+        scores, ib.fix_rows, ib.dev_i64 + 1);
     note_launch();
   }
-  if ((e = cudaMemsetAsync(ib.dev_i64 + 1, 0, 8, s))) return fail(e, "fix count");
-  cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
-  init_merge<<<unsigned(std::min<int64_t>((n + 7) / 8, int64_t(sms) * 16)), 256, 0, s>>>(
-      n, T, K, perm, ib.pos, ib.leaf_lo, ib.leaf_sz, ib.gram, ids, scores, ib.fix_rows, ib.dev_i64 + 1);
-  note_launch();
   int64_t nfix = 0;
   unsigned gflag = 0;
   if ((e = cudaMemcpyAsync(&nfix, ib.dev_i64 + 1, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "fix count");

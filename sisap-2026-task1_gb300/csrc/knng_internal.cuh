@@ -92,12 +92,17 @@ int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t 
 // roots_with_split = number of jobs with n[b] > leaf (their T roots are split)
 
 // ---- init.cu ----
+// The initial-graph stage computes leaf Gram rows for kInitTreeChunk trees at
+// a time (64 int32 per position: 512 B per row for two trees instead of
+// 4 KB for sixteen), merging each chunk into the rows' lists.
+constexpr int kInitTreeChunk = 2;
+inline int init_gram_trees(int T) { return T < kInitTreeChunk ? T : kInitTreeChunk; }
 struct InitBufs {
   int32_t* pos;       // [T*n] inverse permutation (absolute positions)
   int32_t* leaf_lo;   // [T*n] leaf start of each position
   uint8_t* leaf_sz;   // [T*n] leaf size of each position
   int32_t* leaf_idx;  // [T*n] scan scratch
-  int32_t* gram;      // [T*n][leaf] int32 leaf Gram rows
+  int32_t* gram;      // [init_gram_trees(T) * n][64] int32 leaf Gram rows of one chunk of trees
   int32_t* fix_rows;  // [n] rows whose candidate pool is smaller than K
   int64_t* dev_i64;   // [4]
   void* scan_tmp;
@@ -109,9 +114,11 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
              const JobTable& jt, int gram_mode = 0, int wait_limit = 0);
 // gram_mode 0: dp4a leaf Gram (leaf_gram); 1: tcgen05 bf16 tensor-core Gram (leaf_gram_tc)
 // wait_limit: knng_params::wait_limit (0 = default polls per bounded wait)
+// Gram rows of the leaves [leaf_start, leaf_start + nleaves) (the last one ends
+// at position `total`) go to gram[(position - gram_pos0) * 64 ...].
 cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm, const int32_t* leaf_start,
-                                int64_t nleaves, int64_t total, int32_t* gram, unsigned* err, int num_sms,
-                                cudaStream_t s, int wait_limit = 0);
+                                int64_t nleaves, int64_t total, int32_t* gram, int64_t gram_pos0, unsigned* err,
+                                int num_sms, cudaStream_t s, int wait_limit = 0);
 
 // Random initial graph (init_mode KNNG_INIT_RANDOM); every job needs n > K.
 cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int K, uint32_t seed, const JobTable& jt,
@@ -134,13 +141,16 @@ struct JoinCtl {
   int* all_done;                  // [1]
   int* final_buf;                 // [1]: buffer index holding every job's final graph
   long long* upd_log;             // [max_iter][count]: updates per iteration per job
-  // Per-row candidate cache (all null: none).  Row i keeps its previous
+  // Per-row candidate cache (null: none).  Row i keeps its previous
   // iteration's distinct two-hop ids with their Hamming scores and whether the
   // dot is known to be <= the row's pool threshold (which never falls), so the
   // next iteration gathers sketches and code rows only for new candidates.
-  int32_t* cache_ids;             // [n][cache_cap]
-  uint16_t* cache_hr;             // [n][cache_cap]: score << 1 | rejected
-  int* cache_cnt;                 // [n]: entries held (0 before the first iteration)
+  // One word per entry: (job-local id << 9) | (rejected << 8) | (h - base),
+  // with base = that iteration's selection threshold - 160 (at least 0); ids
+  // whose score falls outside [base, base + 255] are not kept.  Job-local ids
+  // need jobs of fewer than 2^23 rows (otherwise the build runs without it).
+  uint32_t* cache_ent;            // [n][cache_cap]
+  int* cache_cnt;                 // [n]: base << 16 | entries (0 before the first iteration)
   int cache_cap;
   int64_t row_limit;              // rows processed (the first ones in visit order); 0: all
   // Unchanged-row skip of double-buffered iterations (both null: none).
@@ -150,12 +160,11 @@ struct JoinCtl {
   uint8_t* chg_out;
 };
 // Entries per row of the candidate cache (rows with more distinct candidates
-// keep the first ones; the rest are scored again) and its bytes for n rows.
+// keep the first ones; the rest are scored again), its bytes for n rows, and
+// the largest job it serves (entries hold 23-bit job-local ids).
 constexpr int kCacheCap = 1536;
-inline size_t cache_bytes(int64_t n) {
-  return ((size_t(n) * kCacheCap * 4 + 255) & ~size_t(255)) + ((size_t(n) * kCacheCap * 2 + 255) & ~size_t(255)) +
-         size_t(n) * 4;
-}
+constexpr int64_t kCacheMaxJobRows = int64_t(1) << 23;
+inline size_t cache_bytes(int64_t n) { return ((size_t(n) * kCacheCap * 4 + 255) & ~size_t(255)) + size_t(n) * 4; }
 cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, int d, int K, int R,
                         const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out,
                         int32_t* scores_out, const int32_t* row_order, unsigned long long* counters,
