@@ -234,6 +234,35 @@ def same_sample_gpu(dev, steps, warmup, sample=CPU_SAMPLE, seed=4242):
             "sample": f"{n} x {d} rows, {c} centres, seed {seed}: the reference arm's own sample", "steps": steps}
 
 
+def reference_recall_same_rows(x, knns, rows):
+    """The reference algorithm (the oracle's restatement of src/main.cpp, its
+    own tie rules and in-place race, every host thread) on exactly the rows the
+    GPU built: recall@15 of both graphs on the same seeded sample against exact
+    float64 brute force, and the CPU build time."""
+    import torch
+
+    import evaluate
+    import synth
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    threads = os.cpu_count() or 1
+    xh = x.cpu().numpy()
+    t0 = time.perf_counter()
+    kr, _, st = oracle.build_graph(xh, oracle.params(threads=threads))
+    cpu_s = time.perf_counter() - t0
+    del xh
+    n = x.shape[0]
+    idx = torch.randperm(n, generator=torch.Generator().manual_seed(7))[: min(rows, n)].numpy()
+    gt = evaluate.sample_knn(x, idx, 15)
+    r_ref = synth.recall_at_k(kr, gt, rows=idx)
+    r_gpu = synth.recall_at_k(knns.cpu().numpy(), gt, rows=idx)
+    return {"n": int(n), "sample_rows": int(len(idx)), "reference_port": r_ref, "gpu": r_gpu,
+            "gap_pt": 100 * (r_ref - r_gpu), "reference_iterations": int(st.iterations),
+            "reference_build_s": float(st.build_s), "reference_wall_s": cpu_s, "threads": threads}
+
+
 def cpu_ref_step(threads, sample=CPU_SAMPLE, seed=4242):
     """One build by the unmodified reference binary (oracle/_ref/main: src/main.cpp
     compiled with its own flags against the container-file H5Cpp shim) on the
@@ -334,21 +363,27 @@ def measure_batched(steps, warmup, seq_passes):
             res, _ = ctx.build_batch(xs)
         bt = []
         launches = 0
+        stages = ("quantize_s", "forest_s", "init_s", "join_s", "export_s")
         with ClockSampler(0) as clk:
             for _ in range(steps):
                 st = knng.Stats()
                 res, st = ctx.build_batch(xs, st)
                 bt.append(st.device_s)
                 launches += st.kernel_launches
+        b_stage = {k[:-2]: getattr(st, k) for k in stages}  # summed over the batch's dimension groups
         for x in xs:
             ctx.build(x)  # warm the plain path too (autotune buckets, buffers)
         seq = []
         same = True
+        s_stage = {}
         for _ in range(seq_passes):
             tot = 0.0
+            s_stage = {k[:-2]: 0.0 for k in stages}
             for j, x in enumerate(xs):
                 k, d_, st1 = ctx.build(x)
                 tot += st1.device_s
+                for k2 in stages:
+                    s_stage[k2[:-2]] += getattr(st1, k2)
                 same &= bool(torch.equal(k, res[j][0]) and torch.equal(d_, res[j][1]))
             seq.append(tot)
     del xs
@@ -359,7 +394,9 @@ def measure_batched(steps, warmup, seq_passes):
             "jobs_per_s": b_js, "ms_per_step": 1e3 * statistics.mean(bt), "steps": steps,
             "sequential_plain_jobs_per_s": s_js, "batched_over_sequential": b_js / s_js,
             "identical_to_plain": same, "vectors_per_s": rows / statistics.mean(bt), "clocks": clk.summary(),
-            "gpu_launches": launches}
+            "gpu_launches": launches,
+            "stage_s": {"batched (sum over dimension groups, which run concurrently)": b_stage,
+                        "sequential (sum over the 64 builds)": s_stage}}
 
 
 def run_batched(args):
@@ -546,6 +583,11 @@ def run_gpu(args):
                         "sketch plus R rows per row, an upper bound the kernel avoids by deduplicating"}
     # ---- recall on a seeded sample
     rec = recall_sample(x, knns, rows=args.recall_rows) if args.recall_rows > 0 and rank == 0 else None
+    # ---- the reference algorithm on these very rows (optional: minutes of CPU
+    #      time at full size): recall@15 of both graphs on the same sample
+    full_parity = None
+    if args.reference_recall and rank == 0:
+        full_parity = reference_recall_same_rows(x, knns, args.recall_rows)
     # ---- the same build on the reference arm's own sample rows (like-for-like N)
     # (part of the CPU-baseline leg: --skip-cpu leaves both out)
     same = same_sample_gpu(dev, args.steps, max(1, args.warmup)) if rank == 0 and ws == 1 and not args.skip_cpu else None
@@ -584,6 +626,7 @@ def run_gpu(args):
                         "join": last.join_s, "export": last.export_s},
             "recall@15": rec, "recall_rows": args.recall_rows, "recall_parity_100k": parity,
             "value_same_config": same["value"] if same else None, "same_config": same,
+            "recall_parity_same_rows": full_parity,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clk.summary(), "gpu_launches": launches, "wall_s": wall,
         }
@@ -616,6 +659,9 @@ def main():
     ap.add_argument("--recall-rows", type=int, default=10_000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--reference-recall", action="store_true",
+                    help="also build the same rows with the reference algorithm on the CPU (minutes at full size) "
+                         "and report both recalls on the same sample")
     ap.add_argument("--skip-forms", action="store_true",
                     help="leave the batched and serving measurements out of the default line")
     ap.add_argument("--traffic-per-launch", type=float, default=None,
