@@ -74,8 +74,7 @@ typedef struct knng_params {
   int join_cache;        /* 1: each row keeps its previous iteration's distinct candidates with
                             their Hamming scores and known rejections (n * 6 KB of device
                             memory), so later iterations skip most sketch and row gathers;
-                            results are identical either way.  0: no cache.  Jobs of 2^23
-                            rows or more build without it. */
+                            results are identical either way.  0: no cache. */
   int block_size;        /* KNNG_INIT_BLOCK: rows per block; each job is split into
                             max(1, round(n / block_size)) equal consecutive blocks (10000:
                             the archive's 200000 rows / 20 blocks, nndescent_hybrid.cpp:20-21) */

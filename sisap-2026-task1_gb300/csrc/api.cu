@@ -102,7 +102,7 @@ struct knng_ctx {
   cudaEvent_t copied[2] = {}, freed[2] = {};
   cudaEvent_t itev[kMaxIterEvents] = {};
   std::string last_error;
-  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs, cache, hsketch, rowflags;
+  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs, hsketch, rowflags;
   // join phase captured as a CUDA graph, reused while the launch key matches
   cudaGraphExec_t join_graph = nullptr;
   std::vector<uintptr_t> join_graph_key;
@@ -111,8 +111,8 @@ struct knng_ctx {
   std::map<std::pair<int, int>, JoinCfg> tuned;
   std::vector<knng_ctx*> subs;  // contexts of the second and later dimension groups of a batch
   std::vector<DevBuf*> buffers() {
-    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs, &cache,
-            &hsketch, &rowflags};
+    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs, &hsketch,
+            &rowflags};
   }
   // the sketches the join scores and their 64-bit words per row
   bool hyperplane() const { return prm.sketch_mode == KNNG_SKETCH_HYPERPLANE; }
@@ -181,13 +181,14 @@ size_t carve(char*& p, size_t bytes) {
 }
 
 // Lays the forest or the init scratch over the ctx scratch region (the two are
-// never live at the same time).
-int ensure_scratch(knng_ctx* c, int64_t n, Scratch* s, int64_t n_replay) {
+// never live at the same time); the region is at least min_bytes long (the
+// candidate cache, which a build lays over it after the initial graph).
+int ensure_scratch(knng_ctx* c, int64_t n, Scratch* s, int64_t n_replay, size_t min_bytes = 0) {
   const int T = c->prm.num_trees, L = c->prm.leaf_size;
   int64_t mn = 0, mt = 0;
   const size_t fbytes = forest_bytes(n, T, L, &mn, &mt) + size_t(n_replay) * 24 + 8192;
   const size_t ibytes = init_bytes(n, T, L) + 8192;
-  cudaError_t e = c->scratch.ensure(std::max(fbytes, ibytes));
+  cudaError_t e = c->scratch.ensure(std::max(std::max(fbytes, ibytes), min_bytes));
   if (e) return cuda_fail(c, e, "scratch allocation");
   e = c->scalars.ensure(4096);
   if (e) return cuda_fail(c, e, "scalar allocation");
@@ -213,7 +214,6 @@ int ensure_scratch(knng_ctx* c, int64_t n, Scratch* s, int64_t n_replay) {
   {
     char* p = c->scratch.as<char>();
     InitBufs& b = s->ib;
-    b.gram = reinterpret_cast<int32_t*>(p); carve(p, size_t(init_gram_trees(T)) * size_t(n) * kMaxLeaf * 4);
     b.pos = reinterpret_cast<int32_t*>(p); carve(p, tn * 4);
     b.leaf_lo = reinterpret_cast<int32_t*>(p); carve(p, tn * 4);
     b.leaf_idx = reinterpret_cast<int32_t*>(p); carve(p, tn * 8);
@@ -221,6 +221,11 @@ int ensure_scratch(knng_ctx* c, int64_t n, Scratch* s, int64_t n_replay) {
     b.fix_rows = reinterpret_cast<int32_t*>(p); carve(p, size_t(n) * 4);
     b.scan_tmp = p; carve(p, scan_tmp_bytes(int64_t(tn)));
     b.dev_i64 = c->scalars.as<int64_t>(128);
+    // the leaf Gram rows take the rest of the region: at least one chunk of
+    // init_gram_trees(T) trees (init_bytes), more when the region was sized
+    // for the candidate cache
+    b.gram = reinterpret_cast<int32_t*>(p);
+    b.gram_rows = int64_t((c->scratch.bytes - size_t(p - c->scratch.as<char>())) / (kMaxLeaf * 4));
   }
   return KNNG_OK;
 }
@@ -431,7 +436,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
       (e = c->leaf_flag.ensure(size_t(T) * N)) || (c->hyperplane() && (e = c->hsketch.ensure(size_t(N) * 16))))
     return cuda_fail(c, e, "device allocation");
   Scratch s;
-  int st = ensure_scratch(c, N, &s, 0);
+  int st = ensure_scratch(c, N, &s, 0, (p.join_cache && MI > 0) ? cache_bytes(N) : 0);
   if (st) return st;
   // job table + NN-Descent control block
   const size_t jb = size_t(J);
@@ -463,7 +468,8 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   ctl.all_done = c->jobs.as<int>(o_flags);
   ctl.final_buf = c->jobs.as<int>(o_flags) + 1;
   ctl.upd_log = c->jobs.as<long long>(o_log);
-  ctl.cache_ent = nullptr;
+  ctl.cache_ids = nullptr;
+  ctl.cache_hr = nullptr;
   ctl.cache_cnt = nullptr;
   ctl.cache_cap = 0;
   ctl.row_limit = 0;  // every row
@@ -471,13 +477,14 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   ctl.chg_out = nullptr;
   const bool skip_rows = p.join_mode == KNNG_JOIN_JACOBI && MI > 0;
   if (skip_rows && (e = c->rowflags.ensure(size_t(2) * size_t(N)))) return cuda_fail(c, e, "row flag allocation");
-  int64_t max_job = 0;
-  for (int b = 0; b < J; ++b) max_job = std::max<int64_t>(max_job, hn[b]);
-  if (p.join_cache && MI > 0 && max_job < kCacheMaxJobRows) {
-    if ((e = c->cache.ensure(cache_bytes(N)))) return cuda_fail(c, e, "candidate cache allocation");
-    char* cp = c->cache.as<char>();
-    ctl.cache_ent = reinterpret_cast<uint32_t*>(cp);
-    cp += (size_t(N) * kCacheCap * 4 + 255) & ~size_t(255);
+  if (p.join_cache && MI > 0) {
+    // over the forest and initial-graph scratch (sized for both by
+    // ensure_scratch): that scratch is dead from the autotune on
+    char* cp = c->scratch.as<char>();
+    ctl.cache_ids = reinterpret_cast<int32_t*>(cp);
+    cp += cache_ids_bytes(N);
+    ctl.cache_hr = reinterpret_cast<uint16_t*>(cp);
+    cp += cache_hr_bytes(N);
     ctl.cache_cnt = reinterpret_cast<int*>(cp);
     ctl.cache_cap = kCacheCap;
   }
@@ -523,10 +530,11 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   // rows in tree-0 leaf order (no forest with the random or block init: natural order)
   const int32_t* order = (p.row_order == KNNG_ORDER_LEAF && forest_init) ? c->perm.as<int32_t>() : nullptr;
   JoinCtl tune_ctl{};  // the candidate cache alone, for the second autotune sweep
-  tune_ctl.cache_ent = ctl.cache_ent;
+  tune_ctl.cache_ids = ctl.cache_ids;
+  tune_ctl.cache_hr = ctl.cache_hr;
   tune_ctl.cache_cnt = ctl.cache_cnt;
   tune_ctl.cache_cap = ctl.cache_cap;
-  const JoinCfg cfg = autotune_join(c, N, d, ids, scs, order, tune_counters, ctl.cache_ent ? &tune_ctl : nullptr);
+  const JoinCfg cfg = autotune_join(c, N, d, ids, scs, order, tune_counters, ctl.cache_ids ? &tune_ctl : nullptr);
   cudaEventRecord(c->ev[3], str);
   // every row starts the phase with an empty candidate cache, and counts as
   // changed before the first iteration
@@ -541,7 +549,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   const char* step = "";
   if (p.use_graph) {
     const std::vector<uintptr_t> key = {uintptr_t(c->codes.p), uintptr_t(c->join_sketch()), uintptr_t(c->graph.p),
-                                        uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(ctl.cache_ent),
+                                        uintptr_t(c->jobs.p), uintptr_t(c->perm.p), uintptr_t(ctl.cache_ids),
                                         uintptr_t(c->rowflags.p),
                                         uintptr_t(N), uintptr_t(d),
                                         uintptr_t(J), uintptr_t(o), uintptr_t(cfg.early.first), uintptr_t(cfg.early.second),
@@ -887,11 +895,14 @@ int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on
   const size_t f = forest_bytes(n, T, q.leaf_size, &mn, &mt);
   const size_t in = init_bytes(n, T, q.leaf_size);
   size_t b = size_t(n) * d + size_t(n) * (d / 64) * 8 + size_t(n) * K * 16 + size_t(T) * n * 5;
-  b += std::max(f, in) + 64 * 1024;
+  // the scratch region holds the forest, then the initial-graph scratch, then
+  // the per-row candidate cache: the largest of the three
+  const size_t cache = (q.join_cache && q.max_iterations > 0) ? cache_bytes(n) : 0;
+  b += std::max(std::max(f, in), cache) + 64 * 1024;
   b += size_t(n) * q.k_eval * 8;                                   // export buffer
   b += size_t(q.max_iterations + 1) * 96 * 8 + 4096;               // control block (per job, bounded)
   if (q.join_mode == KNNG_JOIN_JACOBI) b += size_t(2) * n;          // row-change flags
-  if (q.join_cache && q.max_iterations > 0 && n < kCacheMaxJobRows) b += cache_bytes(n);  // candidate cache
+
   if (q.sketch_mode == KNNG_SKETCH_HYPERPLANE) b += size_t(n) * 16;  // hyperplane sketches
   if (!rows_on_device) b += size_t(2) * std::min<int64_t>(kStageRows, n) * d * 4;  // host-input staging
   return int64_t(b) + (int64_t(1) << 24);                          // pool rounding slack

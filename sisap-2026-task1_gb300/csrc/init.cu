@@ -547,10 +547,13 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
   const size_t gram_smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
   if (gram_mode != 1 && (e = ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram), gram_smem)))
     return fail(e, "gram smem");
-  // kInitTreeChunk trees at a time: their leaf Gram rows (the scratch holds
-  // that many trees' worth), then the merge of those rows into the lists
-  for (int t0 = 0; t0 < T; t0 += kInitTreeChunk) {
-    const int t1 = std::min(T, t0 + kInitTreeChunk);
+  // as many trees at a time as the Gram region holds (at least
+  // init_gram_trees(T)): their leaf Gram rows, then the merge of those rows
+  // into the lists
+  const int chunk = ib.gram_rows > 0 ? int(std::max<int64_t>(1, std::min<int64_t>(T, ib.gram_rows / n)))
+                                      : init_gram_trees(T);
+  for (int t0 = 0; t0 < T; t0 += chunk) {
+    const int t1 = std::min(T, t0 + chunk);
     const int64_t l0 = lt[t0], l1 = lt[t1];
     const int64_t pos0 = int64_t(t0) * n, pos1 = int64_t(t1) * n;
     if (l1 > l0) {

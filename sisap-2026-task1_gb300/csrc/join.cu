@@ -82,12 +82,12 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kGroups = kThreads / 8;  // 8-lane groups per CTA
 constexpr int kHBins = 1025;
+static_assert(kHBins * 4 >= kCacheCap * 2, "the histogram region stages the cached scores");
 constexpr int32_t kEmpty = 0x7fffffff;     // never a valid id (num_trees * n < 2^31)
 constexpr uint32_t kPoolFlag = 0x80000000u; // key bit: id is in the starting list with a real score
 constexpr uint32_t kFirstMask = 0x1fffu;    // meta bits 0..12: first j (8191 = none); 16..26: Hamming score
 constexpr uint32_t kKnown = 0x80000000u;    // meta bit 31: Hamming score taken from the row's candidate cache
 constexpr uint32_t kRej = 0x40000000u;      // meta bit 30: dot known to be <= the row's pool threshold
-constexpr int kCacheBelow = 160;            // the cached score window starts this far below the threshold
 
 struct JoinSmem {
   int K, R, KK, d, W, HT;
@@ -116,7 +116,7 @@ __host__ __device__ inline JoinSmem join_smem(int K, int R, int d) {
   s.o_ulist = o;   o = align16(o + size_t(s.KK) * 2);
   const size_t u0 = o;  // stage C's miss list shares this region with stages F-H
   s.o_surv = o;    o = align16(o + size_t(R) * 16);  // survivors {visit key, dot, id, flags}
-  s.o_miss = u0;  // also stages the row's cache entries (kCacheCap * 4 bytes) before stage B2
+  s.o_miss = u0;  // also stages the row's cached ids (kCacheCap * 4 bytes) before stage B2
   if (o < align16(u0 + size_t(s.KK) * 2)) o = align16(u0 + size_t(s.KK) * 2);
   if (o < align16(u0 + size_t(kCacheCap) * 4)) o = align16(u0 + size_t(kCacheCap) * 4);
   s.o_pool_id = o; o = align16(o + size_t(K) * 4);
@@ -194,19 +194,20 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   int16_t* ulist = reinterpret_cast<int16_t*>(smem + L.o_ulist);
   int16_t* need = cand_slot;  // stage F: the occurrence slots are dead after stage E
   int16_t* misslist = reinterpret_cast<int16_t*>(smem + L.o_miss);  // shares its region with need..order
-  const uint32_t* stage_ent = reinterpret_cast<const uint32_t*>(smem + L.o_miss);  // stage A..B2, same region
+  const int32_t* stage_id = reinterpret_cast<const int32_t*>(smem + L.o_miss);  // stage A..B2, same region
+  const uint16_t* stage_hr = reinterpret_cast<const uint16_t*>(smem + L.o_hist);  // stage A..B2
   int4* surv = reinterpret_cast<int4*>(smem + L.o_surv);
   uint16_t* order = reinterpret_cast<uint16_t*>(cand_slot);  // serial insertion, after stage F
   int32_t* pool_id = reinterpret_cast<int32_t*>(smem + L.o_pool_id);
   int32_t* pool_sc = reinterpret_cast<int32_t*>(smem + L.o_pool_sc);
-  __shared__ int s_cnt, s_ht, s_gt, s_jcut, s_nu, s_nneed, s_nprom, s_nmiss, s_ccnt, s_cw;
+  __shared__ int s_cnt, s_ht, s_gt, s_jcut, s_nu, s_nneed, s_nprom, s_nmiss, s_ccnt;
   __shared__ int32_t s_wsum[kWarps], s_wsum2[kWarps];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, sub = lane & 7, slot8 = lane >> 3;
   const int KK = L.KK, nchunk = d / 16, sk_chunks = W / 2;  // W: sketch words per row (<= L.W = d / 64)
   const uint32_t mask = uint32_t(L.HT - 1);
   const bool inplace = ids_out == ids_in;
-  const bool cached = ctl.cache_ent != nullptr;
+  const bool cached = ctl.cache_ids != nullptr;
   // per-CTA statistics, kept by thread 0 in shared memory (no registers held
   // across the row loop): updates, sketches scored, rows reranked, distinct
   // candidates, rows skipped
@@ -225,10 +226,8 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     const int64_t i = next_i;
     if (r + gridDim.x < nrows) next_i = row_order ? int64_t(row_order[r + gridDim.x]) : r + gridDim.x;
     int job = 0;
-    int64_t job_off = 0;  // cache entries hold job-local ids
     if (ctl.job_done) {
       job = job_of(jt, i);
-      job_off = jt.off[job];
       if (job != flag_job) {
         flag_job = job;
         flag_done = ctl.job_done[job];
@@ -255,7 +254,8 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       if (ctl.chg_in) moved |= (id < 0 || id >= n) ? 1 : int(ctl.chg_in[id]);
     }
     if (ctl.chg_in && tid == 0) moved |= int(ctl.chg_in[i]);
-    for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;
+    if (!cached)
+      for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;
     for (int t = tid; t < L.HT / 4; t += kThreads) {
       reinterpret_cast<uint4*>(key)[t] = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
       reinterpret_cast<uint4*>(meta)[t] = make_uint4(kFirstMask, kFirstMask, kFirstMask, kFirstMask);
@@ -265,7 +265,6 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       s_nu = 0;
       s_nneed = 0;
       s_nprom = 0;
-      s_cw = 0;
       s_ccnt = cached ? ctl.cache_cnt[i] : 0;
     }
     if (__syncthreads_or(moved) == 0) {  // block-uniform
@@ -282,13 +281,17 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     for (int c = tid; c < nchunk; c += kThreads) my_code[c] = reinterpret_cast<const uint4*>(codes + i * d)[c];
     for (int c = tid; c < sk_chunks; c += kThreads) my_sk[c] = reinterpret_cast<const uint4*>(sketch + i * W)[c];
     if (cached) {
-      // stage the row's cache entries into shared memory (over the region of
-      // stages C-H) while stage B runs; the rows' cache slices are 16-byte
-      // aligned and sized for cache_cap
-      const int cc = min(s_ccnt & 0xffff, ctl.cache_cap);
-      const int n_ent = (cc * 4 + 15) / 16;
-      const char* gent = reinterpret_cast<const char*>(ctl.cache_ent + i * ctl.cache_cap);
-      for (int t = tid; t < n_ent; t += kThreads) cp_async16(smem + L.o_miss + 16 * t, gent + 16 * t);
+      // stage the row's cache entries into shared memory (ids over the region
+      // of stages F-H, scores over the histogram) while stage B runs; the
+      // rows' cache slices are 16-byte aligned and sized for cache_cap
+      const int cc = min(s_ccnt, ctl.cache_cap);
+      const int n_id = (cc * 4 + 15) / 16, n_hr = (cc * 2 + 15) / 16;
+      const char* gid = reinterpret_cast<const char*>(ctl.cache_ids + i * ctl.cache_cap);
+      const char* ghr = reinterpret_cast<const char*>(ctl.cache_hr + i * ctl.cache_cap);
+      for (int t = tid; t < n_id + n_hr; t += kThreads) {
+        if (t < n_id) cp_async16(smem + L.o_miss + 16 * t, gid + 16 * t);
+        else cp_async16(smem + L.o_hist + 16 * (t - n_id), ghr + 16 * (t - n_id));
+      }
       cp_async_commit();
     }
     int irregular = 0;
@@ -357,16 +360,17 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     const int16_t* clist = ulist;
     int ncl = nu;
     if (cached) {
-      const int cc = min(s_ccnt & 0xffff, ctl.cache_cap);
-      const uint32_t base = uint32_t(s_ccnt) >> 16;
+      const int cc = min(s_ccnt, ctl.cache_cap);
       for (int q = tid; q < cc; q += kThreads) {
-        const uint32_t e = stage_ent[q];
-        const int sl = table_find(key, mask, int32_t(int64_t(e >> 9) + job_off));
-        if (sl >= 0)
-          meta[sl] = kKnown | ((e & 256u) ? kRej : 0u) | ((base + (e & 255u)) << 16) | (meta[sl] & kFirstMask);
+        const int sl = table_find(key, mask, stage_id[q]);
+        if (sl >= 0) {
+          const uint32_t hr = stage_hr[q];
+          meta[sl] = kKnown | ((hr & 1u) ? kRej : 0u) | (uint32_t(hr >> 1) << 16) | (meta[sl] & kFirstMask);
+        }
       }
       if (tid == 0) s_nmiss = 0;
       __syncthreads();
+      for (int h = tid; h < kHBins; h += kThreads) hist[h] = 0;  // the staged scores are consumed
       for (int q0 = warp * 32; q0 < nu; q0 += kThreads) {
         const int q = q0 + lane;
         const int sl = q < nu ? int(ulist[q]) : -1;
@@ -554,33 +558,18 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
     }
     __syncthreads();
     // ---- F3  the row's cache for the next iteration: this iteration's distinct
-    //          candidates whose score lies in the window [base, base + 255]
-    //          around the selection threshold (base = h_t - kCacheBelow), up
-    //          to cache_cap of them, one word each: (job-local id << 9) |
-    //          (rejected << 8) | (h - base).  Candidates outside the window
-    //          are scored again next time; the count and base are written
-    //          after the next barrier.
-    if (cached && s_ht >= 0) {  // block-uniform (every occurrence selected: nothing worth caching)
-      const int base = max(0, s_ht - kCacheBelow);
-      uint32_t* ce = ctl.cache_ent + i * ctl.cache_cap;
-      for (int q0 = warp * 32; q0 < nu; q0 += kThreads) {  // warp-uniform trip count
-        const int q = q0 + lane;
-        bool keep = false;
-        uint32_t e = 0;
-        if (q < nu) {
-          const int sl = ulist[q];
-          const uint32_t m = meta[sl];
-          const int h = int((m >> 16) & 0x7ffu);
-          keep = h >= base && h <= base + 255;
-          e = (uint32_t(int64_t(uint32_t(key[sl]) & 0x7fffffffu) - job_off) << 9) | ((m & kRej) ? 256u : 0u) |
-              uint32_t(h - base);
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, keep);
-        int at = 0;
-        if (lane == 0 && bal) at = atomicAdd(&s_cw, __popc(bal));
-        at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
-        if (keep && at < ctl.cache_cap) ce[at] = e;
+    //          candidates (the first cache_cap of them) with score and flag
+    if (cached) {
+      const int cc = min(nu, ctl.cache_cap);
+      int32_t* cid = ctl.cache_ids + i * ctl.cache_cap;
+      uint16_t* chr = ctl.cache_hr + i * ctl.cache_cap;
+      for (int q = tid; q < cc; q += kThreads) {
+        const int sl = ulist[q];
+        const uint32_t m = meta[sl];
+        cid[q] = int32_t(uint32_t(key[sl]) & 0x7fffffffu);
+        chr[q] = uint16_t((((m >> 16) & 0x7ffu) << 1) | ((m & kRej) ? 1u : 0u));
       }
+      if (tid == 0) ctl.cache_cnt[i] = cc;
     }
     // ---- G/H  insertion of the survivors in visit order (pkey descending;
     //   keys are distinct).  The new pool goes to new_id/new_sc, laid over the
@@ -718,9 +707,6 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       for (int o = 16; o > 0; o >>= 1) changed += __shfl_xor_sync(full, changed, o);
       if (lane == 0) s_stat[0] += unsigned(changed);
       if (ctl.chg_out && lane == 0) ctl.chg_out[i] = changed ? 1 : 0;
-      if (cached && lane == 0)
-        ctl.cache_cnt[i] = s_ht >= 0 ? int((uint32_t(max(0, s_ht - kCacheBelow)) << 16) | uint32_t(min(s_cw, ctl.cache_cap)))
-                                     : 0;
       if (ctl.job_upd && lane == 0) {
         if (job != run_job) {
           if (run_job >= 0 && run_upd) atomicAdd(ctl.job_upd + run_job, run_upd);

@@ -102,7 +102,9 @@ struct InitBufs {
   int32_t* leaf_lo;   // [T*n] leaf start of each position
   uint8_t* leaf_sz;   // [T*n] leaf size of each position
   int32_t* leaf_idx;  // [T*n] scan scratch
-  int32_t* gram;      // [init_gram_trees(T) * n][64] int32 leaf Gram rows of one chunk of trees
+  int32_t* gram;      // [gram_rows][64] int32 leaf Gram rows of one chunk of trees
+  int64_t gram_rows = 0;  // rows the gram region holds (0: init_gram_trees(T) * n); a chunk is as
+                          // many trees as fit
   int32_t* fix_rows;  // [n] rows whose candidate pool is smaller than K
   int64_t* dev_i64;   // [4]
   void* scan_tmp;
@@ -141,16 +143,13 @@ struct JoinCtl {
   int* all_done;                  // [1]
   int* final_buf;                 // [1]: buffer index holding every job's final graph
   long long* upd_log;             // [max_iter][count]: updates per iteration per job
-  // Per-row candidate cache (null: none).  Row i keeps its previous
+  // Per-row candidate cache (all null: none).  Row i keeps its previous
   // iteration's distinct two-hop ids with their Hamming scores and whether the
   // dot is known to be <= the row's pool threshold (which never falls), so the
   // next iteration gathers sketches and code rows only for new candidates.
-  // One word per entry: (job-local id << 9) | (rejected << 8) | (h - base),
-  // with base = that iteration's selection threshold - 160 (at least 0); ids
-  // whose score falls outside [base, base + 255] are not kept.  Job-local ids
-  // need jobs of fewer than 2^23 rows (otherwise the build runs without it).
-  uint32_t* cache_ent;            // [n][cache_cap]
-  int* cache_cnt;                 // [n]: base << 16 | entries (0 before the first iteration)
+  int32_t* cache_ids;             // [n][cache_cap]
+  uint16_t* cache_hr;             // [n][cache_cap]: score << 1 | rejected
+  int* cache_cnt;                 // [n]: entries held (0 before the first iteration)
   int cache_cap;
   int64_t row_limit;              // rows processed (the first ones in visit order); 0: all
   // Unchanged-row skip of double-buffered iterations (both null: none).
@@ -160,11 +159,13 @@ struct JoinCtl {
   uint8_t* chg_out;
 };
 // Entries per row of the candidate cache (rows with more distinct candidates
-// keep the first ones; the rest are scored again), its bytes for n rows, and
-// the largest job it serves (entries hold 23-bit job-local ids).
+// keep the first ones; the rest are scored again) and its bytes for n rows.
+// The cache lives in the context's scratch buffer, over the forest and
+// initial-graph scratch, which is dead once the initial graph exists.
 constexpr int kCacheCap = 1536;
-constexpr int64_t kCacheMaxJobRows = int64_t(1) << 23;
-inline size_t cache_bytes(int64_t n) { return ((size_t(n) * kCacheCap * 4 + 255) & ~size_t(255)) + size_t(n) * 4; }
+inline size_t cache_ids_bytes(int64_t n) { return (size_t(n) * kCacheCap * 4 + 255) & ~size_t(255); }
+inline size_t cache_hr_bytes(int64_t n) { return (size_t(n) * kCacheCap * 2 + 255) & ~size_t(255); }
+inline size_t cache_bytes(int64_t n) { return cache_ids_bytes(n) + cache_hr_bytes(n) + size_t(n) * 4; }
 cudaError_t launch_join(const int8_t* codes, const uint64_t* sketch, int64_t n, int d, int K, int R,
                         const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out,
                         int32_t* scores_out, const int32_t* row_order, unsigned long long* counters,
