@@ -49,7 +49,7 @@ GRAM = {"dp4a": 0, "tc": 1}
 # DRAM read + write bytes per row of one working NN-Descent launch: the mean
 # over the working join launches of one 300k x 1024 build (3k centres), from
 # the one-pass ncu capture summarised in profiles/join_kernel_dram_300k.md.
-JOIN_DRAM_BYTES_PER_ROW_300K = 18962.0
+JOIN_DRAM_BYTES_PER_ROW_300K = 22251.0
 JOIN_TRAFFIC_SOURCE = ("profiles/join_kernel_dram_300k.md: mean DRAM bytes per row of a 300k build's working "
                        "join launches (ncu), times this workload's rows")
 
