@@ -97,6 +97,11 @@ __device__ __forceinline__ void widen4(uint32_t w, uint32_t& lo, uint32_t& hi) {
   asm("add.f16x2 %0, %1, %2;" : "=r"(hi) : "r"(b), "r"(0xE480E480u));
 }
 
+// Byte offset of 16-byte piece pc (0..3) of row r in a ring slot: rows are
+// 64 bytes apart and the pieces of a row are permuted by (r / 2) % 4, so 8
+// consecutive rows' pieces of one index fall in 8 distinct bank groups.
+__device__ __forceinline__ int ring_offset(int r, int pc) { return r * kChunk + ((pc ^ ((r >> 1) & 3)) << 4); }
+
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
@@ -181,7 +186,7 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
         const int idx = tid + kTcThreads * u;  // 512 pieces of 16 bytes: row idx / 4, piece idx % 4
         const int r = idx >> 2, pc = idx & 3;
         const int32_t id = row_id[b][r];
-        if (id >= 0) cp_async16(dst + r * kChunk + pc * 16, codes + int64_t(id) * d + ic * kChunk + pc * 16);
+        if (id >= 0) cp_async16(dst + ring_offset(r, pc), codes + int64_t(id) * d + ic * kChunk + pc * 16);
       }
       if (++ic == nchunks) {
         ic = 0;
@@ -233,14 +238,20 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
         gave_up = 1;  // pending stays set: the drain waits for that commit
       }
     }
-    if (!gave_up) {  // thread t widens 32 codes of X's row t / 2 into the core-matrix layout
-      const int r = tid >> 1, half = tid & 1;
+    if (!gave_up) {
+      // the warp widens 32 codes of each of 16 rows into the core-matrix
+      // layout: lanes 8h..8h+7 take rows 0-7 (h = 0, 1) or 8-15 (h = 2, 3)
+      // of the warp's 16 and the half h & 1 of the row's 64 codes, so the 8
+      // lanes of every 16-byte access phase touch 8 distinct bank groups in
+      // both the ring and the stage
+      const int r = warp * 16 + (lane & 7) + 8 * (lane >> 4), half = (lane >> 3) & 1;
       const bool live = row_id[b][r] >= 0;
-      const unsigned char* src = ring + slot * kI8Bytes + r * kChunk + half * 32;
+      const unsigned char* src = ring + slot * kI8Bytes;
       unsigned char* dst = stage[st] + (r >> 3) * kSbo + (r & 7) * 16 + half * 4 * 128;
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
-        const uint4 v = live ? *reinterpret_cast<const uint4*>(src + 16 * p) : make_uint4(0, 0, 0, 0);
+        const uint4 v =
+            live ? *reinterpret_cast<const uint4*>(src + ring_offset(r, 2 * half + p)) : make_uint4(0, 0, 0, 0);
         uint4 o0, o1;
         widen4(v.x, o0.x, o0.y);
         widen4(v.y, o0.z, o0.w);
