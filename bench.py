@@ -491,7 +491,8 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     x = synth.mixture_torch(n, d, centres, seed=1000 * 2 + rank, device=dev)
     torch.cuda.synchronize()
-    prm = knng.params(device=local, gram_mode=GRAM[args.gram], join_cache=args.join_cache)
+    prm = knng.params(device=local, gram_mode=GRAM[args.gram], join_cache=args.join_cache,
+                      forest_fuse=args.forest_fuse)
     ctx = knng.Context(prm)
     knns = torch.empty((n, prm.k_eval), dtype=torch.int32, device=dev)
     dists = torch.empty((n, prm.k_eval), dtype=torch.float32, device=dev)
@@ -526,13 +527,19 @@ def run_gpu(args):
         ctx.build(xh, kh, dh)  # warm the host-input path
         grp.barrier()
         e2e_s = 0.0
+        e2e_stats = []
         for _ in range(args.steps):
             st = knng.Stats()
             ctx.build(xh, kh, dh, st)
             e2e_s += st.device_s
+            e2e_stats.append(st)
         e2e_max = grp.max(e2e_s, device=dev)
         e2e = {"value": ws * n * args.steps / e2e_max, "unit": "vectors/s", "h2d_bytes_per_step": n * d * 4,
-               "d2h_bytes_per_step": n * prm.k_eval * 8}
+               "d2h_bytes_per_step": n * prm.k_eval * 8,
+               # quantize reads the pinned host rows over the host link; the
+               # export stage includes the device-to-host copy of knns/dists
+               "stage_s": {f: statistics.mean(getattr(q, f + "_s") for q in e2e_stats)
+                           for f in ("quantize", "forest", "init", "join", "export")}}
         del xh
     # ---- roofline of the dominant kernel (NN-Descent join launches)
     # Algorithmic bytes per row of one iteration of the reference algorithm:
@@ -610,6 +617,7 @@ def run_gpu(args):
                        "k_build": K, "trees": prm.num_trees, "leaf": prm.leaf_size, "rerank": prm.rerank_mult,
                        "join": "jacobi" if prm.join_mode == 0 else "inplace",
                        "leaf_gram": "tcgen05 bf16" if prm.gram_mode == 1 else "dp4a",
+                       "forest": "three levels per pass" if prm.forest_fuse else "one level per pass",
                        "candidate_cache": bool(prm.join_cache),
                        "join_tuned": {"ctas_per_sm": last.join_ctas_per_sm, "cblock": last.join_cblock,
                                       "cuda_graph": bool(last.graph_used)},
@@ -654,6 +662,8 @@ def main():
                     help="leaf Gram: tcgen05 bf16 tensor cores or dp4a")
     ap.add_argument("--join-cache", type=int, default=1, choices=[0, 1],
                     help="per-row candidate cache in the NN-Descent join (identical results; 1 = default)")
+    ap.add_argument("--forest-fuse", type=int, default=1, choices=[0, 1],
+                    help="RP forest: three levels per pass over large nodes (1 = default) or one level per pass")
     ap.add_argument("--serve-jobs", type=int, default=32)
     ap.add_argument("--slots", type=int, default=3)
     ap.add_argument("--recall-rows", type=int, default=10_000)

@@ -95,6 +95,11 @@ typedef struct knng_params {
                             row, the signs of the int8 codes projected on 128 integer
                             hyperplanes drawn from `seed` (the README's random-hyperplane
                             sketch, README.md:33-34; no output of the reference to match) */
+  int forest_fuse;       /* 1 (default): with native pivots, forest nodes of >= 512 members
+                            are split three levels per pass over their code rows, the
+                            descendants' pivots drawn from a seeded, evaluated sample of the
+                            node's members; 0: one level per pass.  A replay table
+                            (knng_forest) always splits one level per pass. */
 } knng_params;
 
 /* Per-build timings and convergence record (seconds, device-timed). */

@@ -159,6 +159,7 @@ int check_params(knng_ctx* c, const knng_params& p) {
     return set_error(c, KNNG_E_ARGS, "join_ctas_per_sm must be 0, or 3 or 4 with join_cblock 2, 4 or 8");
   if (p.sketch_mode != KNNG_SKETCH_SIGN && p.sketch_mode != KNNG_SKETCH_HYPERPLANE)
     return set_error(c, KNNG_E_ARGS, "bad sketch_mode");
+  if (p.forest_fuse != 0 && p.forest_fuse != 1) return set_error(c, KNNG_E_ARGS, "forest_fuse must be 0 or 1");
   return KNNG_OK;
 }
 
@@ -202,12 +203,17 @@ int ensure_scratch(knng_ctx* c, int64_t n, Scratch* s, int64_t n_replay, size_t 
     f.side = reinterpret_cast<uint8_t*>(p); carve(p, tn);
     f.node_a = reinterpret_cast<int32_t*>(p); carve(p, size_t(4 * mn) * 4);
     f.node_b = reinterpret_cast<int32_t*>(p); carve(p, size_t(4 * mn) * 4);
+    f.node_c = reinterpret_cast<int32_t*>(p); carve(p, size_t(4 * mn) * 4);
     f.tile_off = reinterpret_cast<int32_t*>(p); carve(p, size_t(mn + 1) * 4);
     f.child_cnt = reinterpret_cast<int32_t*>(p); carve(p, size_t(mn + 1) * 4);
-    f.tile_left = reinterpret_cast<int32_t*>(p); carve(p, size_t(mt) * 4);
-    f.tile_left_off = reinterpret_cast<int32_t*>(p); carve(p, size_t(mt) * 4);
+    f.child_cnt2 = reinterpret_cast<int32_t*>(p); carve(p, size_t(mn + 1) * 4);
+    f.piv = reinterpret_cast<int32_t*>(p); carve(p, size_t(mn) * 14 * 4);
+    f.tile_bins = reinterpret_cast<int32_t*>(p); carve(p, size_t(8) * mt * 4);
+    f.tile_bins_off = reinterpret_cast<int32_t*>(p); carve(p, size_t(8) * mt * 4);
+    f.tile_left = f.tile_bins;  // the per-level path's tile counts (never live with the fused ones)
+    f.tile_left_off = f.tile_bins_off;
     f.replay_dev = reinterpret_cast<int32_t*>(p); carve(p, size_t(n_replay) * 24 + 16);
-    f.scan_tmp = p; carve(p, scan_tmp_bytes(std::max(mn, mt)));
+    f.scan_tmp = p; carve(p, scan_tmp_bytes(std::max<int64_t>(mn, 8 * mt)));
     f.dev_i64 = c->scalars.as<int64_t>(0);
     f.err = c->scalars.as<unsigned>(64);
   }
@@ -511,7 +517,8 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
       if (hn[b] / nb < K + 1) return set_error(c, KNNG_E_ARGS, "block init needs k_build + 1 rows in every block");
     }
   } else if ((st = run_forest(c->codes.as<int8_t>(), N, d, T, p.leaf_size, p.seed, nullptr, 0, c->perm.as<int32_t>(),
-                              c->leaf_flag.as<uint8_t>(), s.fb, str, &levels, &c->last_error, jt, split))) {
+                              c->leaf_flag.as<uint8_t>(), s.fb, str, &levels, &c->last_error, jt, split,
+                              p.forest_fuse))) {
     return st;
   }
   cudaEventRecord(c->ev[2], str);
@@ -683,6 +690,7 @@ void knng_default_params(knng_params* p) {
   p->join_ctas_per_sm = 0;
   p->join_cblock = 0;
   p->sketch_mode = KNNG_SKETCH_SIGN;
+  p->forest_fuse = 1;
 }
 
 const char* knng_status_string(int s) {
@@ -817,7 +825,7 @@ int knng_forest(knng_ctx* c, const int8_t* codes_dev, int64_t n, int d, const in
   if ((st = single_job(c, n, &jt))) return st;
   st = run_forest(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.seed, replay, replay ? n_replay : 0,
                   perm_dev, leaf_flag_dev, s.fb, c->stream, &levels, &c->last_error, jt,
-                  n > c->prm.leaf_size ? 1 : 0);
+                  n > c->prm.leaf_size ? 1 : 0, c->prm.forest_fuse);
   if (st) return st;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   return e ? cuda_fail(c, e, "forest") : KNNG_OK;

@@ -74,10 +74,15 @@ struct ForestBufs {
   uint8_t* side;          // [T*n]
   int32_t* node_a;        // node arrays, two generations: start,size,p1,p2
   int32_t* node_b;
+  int32_t* node_c;        // nodes parked by the fused rounds for the per-level loop
   int32_t* tile_off;      // [max_nodes + 1]
-  int32_t* tile_left;     // [max_tiles]
-  int32_t* tile_left_off; // [max_tiles]
+  int32_t* tile_left;     // [max_tiles] (per-level path; shares tile_bins)
+  int32_t* tile_left_off; // [max_tiles] (per-level path; shares tile_bins_off)
+  int32_t* tile_bins;     // [8 * max_tiles] fused path: members per tile and path code
+  int32_t* tile_bins_off; // [8 * max_tiles]
+  int32_t* piv;           // [max_nodes * 14] fused path: pivot tables
   int32_t* child_cnt;     // [max_nodes + 1]
+  int32_t* child_cnt2;    // [max_nodes + 1]
   int64_t* dev_i64;       // [4] device scalars
   unsigned* err;          // device error flags
   void* scan_tmp;
@@ -88,8 +93,10 @@ size_t forest_bytes(int64_t n, int T, int leaf, int64_t* max_nodes, int64_t* max
 int run_forest(const int8_t* codes, int64_t n, int d, int T, int leaf, uint32_t seed,
                const int32_t* replay_host, int64_t n_replay, int32_t* perm, uint8_t* leaf_flag,
                const ForestBufs& fb, cudaStream_t s, int64_t* levels_out, std::string* err,
-               const JobTable& jt, int roots_with_split);
-// roots_with_split = number of jobs with n[b] > leaf (their T roots are split)
+               const JobTable& jt, int roots_with_split, int fuse);
+// roots_with_split = number of jobs with n[b] > leaf (their T roots are split);
+// fuse = 1: nodes of >= 512 members split three levels per pass (native
+// pivots only; a replay table always takes the per-level path)
 
 // ---- init.cu ----
 // The initial-graph stage computes leaf Gram rows for kInitTreeChunk trees at

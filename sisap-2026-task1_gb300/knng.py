@@ -42,7 +42,7 @@ class Params(C.Structure):
         ("row_order", C.c_int), ("seed", C.c_uint32), ("device", C.c_int), ("autotune", C.c_int),
         ("use_graph", C.c_int), ("gram_mode", C.c_int), ("init_mode", C.c_int), ("join_cache", C.c_int),
         ("block_size", C.c_int), ("bridges", C.c_int), ("wait_limit", C.c_int), ("join_ctas_per_sm", C.c_int),
-        ("join_cblock", C.c_int), ("sketch_mode", C.c_int),
+        ("join_cblock", C.c_int), ("sketch_mode", C.c_int), ("forest_fuse", C.c_int),
     ]
 
 

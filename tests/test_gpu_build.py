@@ -42,7 +42,10 @@ def _golden(name):
     return x, np.load(os.path.join(HERE, "golden", name + ".npz"))
 
 
-def _check_export(x, knns, dists):
+def _check_export(x, knns, dists, unique_rows=None):
+    """Valid ids (no self), lists sorted, exact int8 scores on a sample of rows,
+    and distinct ids in every sampled row (in the rows of unique_rows only, when
+    given)."""
     n = x.shape[0]
     codes, _ = oracle.quantize(x)
     ids = knns.astype(np.int64) - 1
@@ -52,8 +55,9 @@ def _check_export(x, knns, dists):
     sample = np.arange(0, n, max(1, n // 500))
     exact = np.einsum("id,ikd->ik", codes[sample].astype(np.int32), codes[ids[sample]].astype(np.int32))
     np.testing.assert_array_equal(dists[sample], exact.astype(np.float32))
-    for row in ids[sample]:
-        assert len(np.unique(row)) == len(row)
+    for i in sample:
+        if unique_rows is None or unique_rows[i]:
+            assert len(np.unique(ids[i])) == ids.shape[1], i
 
 
 @pytest.mark.parametrize("name", ["mix_n2000_d1024", "mix_n6000_d1024_c600", "mix_n3000_d384", "mix_n2500_d768",
@@ -194,16 +198,24 @@ def test_build_one_million_properties(knng_mod):
     assert rec > 0.3, rec
 
 
-def test_build_degenerate_duplicates(knng_mod):
+@pytest.mark.parametrize("fuse", [1, 0])
+def test_build_degenerate_duplicates(knng_mod, fuse):
     """All-identical rows: no pivot separates them (every split peels one row, as in
     the reference), the forest's depth valve cuts the tail into leaves, and the
-    graph is still a valid list of distinct ids with exact scores."""
+    graph is still a valid list of ids with exact scores.
+
+    Among the identical rows every score ties, and the reference's initial list
+    keeps an id twice when a random fill repeats a leaf candidate that a tied
+    entry separates from it (it drops only adjacent repeats, src/main.cpp:295-302);
+    no later visit can replace a tied entry.  The reference algorithm (the
+    oracle's restatement) leaves repeated ids in about 1 % of these rows, so the
+    ids are required distinct in the mixture half only."""
     knng = knng_mod
     x = np.tile(synth.mixture(1, 256, 1, seed=3), (5000, 1))
     x[:2500] = synth.mixture(2500, 256, 25, seed=4)  # half duplicates, half mixture
-    with knng.Context() as ctx:
+    with knng.Context(forest_fuse=fuse) as ctx:
         knns, dists, st = ctx.build(np.ascontiguousarray(x))
-    _check_export(x, knns, dists)
+    _check_export(x, knns, dists, unique_rows=np.arange(5000) < 2500)
 
 
 def _oracle_random_build(x, max_iter=30):

@@ -96,15 +96,18 @@ def _check_forest_invariants(perm, lf, n, leaf):
         assert sizes.min() >= 1 and sizes.max() <= leaf
 
 
-@pytest.mark.parametrize("n,d", [(20000, 1024), (3000, 384)])
-def test_forest_native_invariants_and_init(torch_dev, n, d):
+@pytest.mark.parametrize("fuse", [1, 0])
+@pytest.mark.parametrize("n,d", [(20000, 1024), (3000, 384), (120000, 128)])
+def test_forest_native_invariants_and_init(torch_dev, n, d, fuse):
+    """Native pivots, three levels per pass (fuse = 1: two fused rounds and the
+    per-level tail at 20000 rows, more rounds at 120000) or one level per pass."""
     torch, dev = torch_dev
     import knng
 
     x = synth.mixture(n, d, n // 100, seed=7)
     codes_ref, _ = oracle.quantize(x)
     codes = torch.from_numpy(codes_ref).to(dev)
-    with knng.Context() as ctx:
+    with knng.Context(forest_fuse=fuse) as ctx:
         perm, lf = ctx.forest(codes)
         perm_h, lf_h = perm.cpu().numpy(), lf.cpu().numpy()
         _check_forest_invariants(perm_h, lf_h, n, 64)
