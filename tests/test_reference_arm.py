@@ -26,7 +26,9 @@ def _run(monkeypatch, capsys):
                            "d2h_bytes_per_step": 0}
     cb = line["cpu_baseline"]
     assert cb["value"] == line["value"] and cb["cores"] == (os.cpu_count() or 1)
-    assert cb["sample"].startswith("3000 x 1024 rows, 30 centres")
+    assert "3000 x 1024 rows, 30 centres" in cb["sample"]
+    # the same config object as the GPU arm's line, so the two lines compare
+    assert line["config"] == bench.workload_config("full", 1)
     return line
 
 
