@@ -38,7 +38,9 @@ typedef enum knng_status {
   KNNG_E_REPLAY = -7,  /* replay pivot table does not match the forest */
   KNNG_E_BUSY = -8,    /* ticket not finished yet (knng_poll) */
   KNNG_E_NOTFOUND = -9, /* unknown ticket */
-  KNNG_E_SCRATCH = -10  /* input too large for knng_init_graph_noalloc's fixed scratch */
+  KNNG_E_SCRATCH = -10, /* input too large for knng_init_graph_noalloc's fixed scratch */
+  KNNG_E_BOUNDS = -11   /* a device bounds check failed: an id, permutation entry or leaf position
+                           outside its array (bounds-checked build libknng_checked.so only) */
 } knng_status;
 
 enum { KNNG_QUANT_TRUNC = 0, KNNG_QUANT_ROUND = 1 };

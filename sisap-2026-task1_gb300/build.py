@@ -1,12 +1,17 @@
 """Build libknng.so (CUDA, sm_103a) and the knng_main CLI in place.
 
-    python sisap-2026-task1_gb300/build.py [--force]
+    python sisap-2026-task1_gb300/build.py [--force] [--checked]
 
 Each csrc/*.cu compiles to _build/<name>.o in parallel (one -gencode, sm_103a
 only), then nvcc links libknng.so next to this file; host/*.cpp link into
 knng_main against it (rpath $ORIGIN), with zlib (deflate-compressed HDF5
 input) when the host has its header and library.  Targets are rebuilt only
 when a source or header is newer.
+
+--checked builds the bounds-checked library libknng_checked.so instead
+(-DKNNG_CHECKS, objects in _build_checked/): every index a kernel derives from
+its inputs is checked before it addresses memory and a failed check returns
+KNNG_E_BOUNDS.  Load it by setting KNNG_LIBRARY to its path.
 """
 from __future__ import annotations
 
@@ -23,6 +28,8 @@ CSRC = os.path.join(PKG, "csrc")
 HOST = os.path.join(PKG, "host")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libknng.so")
+LIB_CHECKED = os.path.join(PKG, "libknng_checked.so")
+OUT_CHECKED = os.path.join(PKG, "_build_checked")
 CLI = os.path.join(PKG, "knng_main")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
@@ -60,22 +67,32 @@ def _zlib_flags():
     return ["-DKNNG_HAVE_ZLIB", "-lz"] if r.returncode == 0 else []
 
 
-def build(force=False, verbose=False):
-    os.makedirs(OUT, exist_ok=True)
+def _library(out_dir, lib, extra, force, verbose):
+    os.makedirs(out_dir, exist_ok=True)
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     jobs = []
     for src in sources:
-        obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(out_dir, os.path.basename(src)[:-3] + ".o")
         if force or _newer(obj, [src] + headers):
-            jobs.append([nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for r in ex.map(_run, jobs):
             if verbose and r.stderr:
                 print(r.stderr, file=sys.stderr)
-    objs = [os.path.join(OUT, os.path.basename(s)[:-3] + ".o") for s in sources]
-    if force or jobs or _newer(LIB, objs):
-        _run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcublas", "-lcusolver"])  # knng_pca
+    objs = [os.path.join(out_dir, os.path.basename(s)[:-3] + ".o") for s in sources]
+    if force or jobs or _newer(lib, objs):
+        _run([nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcublas", "-lcusolver"])  # knng_pca
+
+
+def build_checked(force=False, verbose=False):
+    """libknng_checked.so: the same library with the device bounds checks compiled in."""
+    _library(OUT_CHECKED, LIB_CHECKED, ["-DKNNG_CHECKS"], force, verbose)
+    return LIB_CHECKED
+
+
+def build(force=False, verbose=False):
+    _library(OUT, LIB, [], force, verbose)
     host_srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
     host_hdrs = glob.glob(os.path.join(HOST, "*.h"))
     if host_srcs and (force or _newer(CLI, host_srcs + host_hdrs + [LIB])):
@@ -86,5 +103,8 @@ def build(force=False, verbose=False):
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
-    print(LIB)
+    if "--checked" in sys.argv:
+        print(build_checked(force="--force" in sys.argv, verbose=True))
+    else:
+        build(force="--force" in sys.argv, verbose=True)
+        print(LIB)

@@ -123,6 +123,10 @@ struct knng_ctx {
 namespace {
 
 constexpr int64_t kStageRows = 1 << 16;  // host-input rows per H2D chunk (256 MB at d = 1024)
+// byte offset in the context's 4096-byte scalar block of the bounds-checked
+// build's error word (the forest uses bytes 0..67, the initial graph 128..159,
+// knng_join_iter's counters 256..319)
+constexpr size_t kCheckWord = 768;
 
 int set_error(knng_ctx* c, int status, const std::string& msg) {
   if (c) c->last_error = msg;
@@ -481,6 +485,10 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   ctl.row_limit = 0;  // every row
   ctl.chg_in = nullptr;  // set per iteration by join_phase
   ctl.chg_out = nullptr;
+  // the bounds-checked build's error word of the join and the export
+  ctl.check_err = kChecked ? c->scalars.as<unsigned>(kCheckWord) : nullptr;
+  if (kChecked && (e = cudaMemsetAsync(ctl.check_err, 0, sizeof(unsigned), str)))
+    return cuda_fail(c, e, "check word reset");
   const bool skip_rows = p.join_mode == KNNG_JOIN_JACOBI && MI > 0;
   if (skip_rows && (e = c->rowflags.ensure(size_t(2) * size_t(N)))) return cuda_fail(c, e, "row flag allocation");
   if (p.join_cache && MI > 0) {
@@ -615,7 +623,7 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
     kd = c->outbuf.as<int32_t>(0);
     dd = c->outbuf.as<float>(outn * 4);
   }
-  if ((e = launch_export(ids[fin], scs[fin], N, K, p.k_eval, nullptr, kd, dd, str, &jt)))
+  if ((e = launch_export(ids[fin], scs[fin], N, K, p.k_eval, nullptr, kd, dd, str, &jt, ctl.check_err)))
     return cuda_fail(c, e, "export");
   if (!direct)
     for (int b = 0; b < J; ++b) {
@@ -626,7 +634,12 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
         return cuda_fail(c, e, "output copy");
     }
   cudaEventRecord(c->ev[5], str);
+  unsigned check = 0;
+  if (kChecked && (e = cudaMemcpyAsync(&check, ctl.check_err, sizeof(unsigned), cudaMemcpyDeviceToHost, str)))
+    return cuda_fail(c, e, "check word");
   if ((e = cudaStreamSynchronize(str))) return cuda_fail(c, e, "build");
+  if (check & kErrBounds)
+    return set_error(c, KNNG_E_BOUNDS, "NN-Descent or export: an id outside [0, n) (bounds check)");
   int max_it = 0;
   for (int b = 0; b < J; ++b) {
     jobs[b].iterations = iters[b];
@@ -706,6 +719,7 @@ const char* knng_status_string(int s) {
     case KNNG_E_BUSY: return "job not finished";
     case KNNG_E_NOTFOUND: return "unknown ticket";
     case KNNG_E_SCRATCH: return "input exceeds the fixed no-allocation scratch";
+    case KNNG_E_BOUNDS: return "a device bounds check failed (bounds-checked build)";
     default: return "unknown status";
   }
 }
@@ -864,12 +878,21 @@ int knng_join_iter(knng_ctx* c, const int8_t* codes_dev, const uint64_t* sketch_
   const int K = c->prm.k_build;
   const int cps = c->prm.join_ctas_per_sm ? c->prm.join_ctas_per_sm : 4;
   const int cb = c->prm.join_ctas_per_sm ? c->prm.join_cblock : 4;
+  JoinCtl chk{};  // no jobs, no cache, no row flags: only the bounds-checked build's error word
+  chk.check_err = kChecked ? c->scalars.as<unsigned>(kCheckWord) : nullptr;
+  if (kChecked && (e = cudaMemsetAsync(chk.check_err, 0, sizeof(unsigned), c->stream)))
+    return cuda_fail(c, e, "check word reset");
   if ((e = launch_join(codes_dev, sketch_dev, n, d, K, K * c->prm.rerank_mult, ids_in, scores_in, ids_out,
-                       scores_out, nullptr, up, c->num_sms, c->stream, nullptr, nullptr, cps, cb, c->sketch_words(d))))
+                       scores_out, nullptr, up, c->num_sms, c->stream, nullptr, kChecked ? &chk : nullptr, cps, cb,
+                       c->sketch_words(d))))
     return cuda_fail(c, e, "join");
   unsigned long long h = 0;
+  unsigned check = 0;
   if ((e = cudaMemcpyAsync(&h, up, 8, cudaMemcpyDeviceToHost, c->stream))) return cuda_fail(c, e, "update count");
+  if (kChecked && (e = cudaMemcpyAsync(&check, chk.check_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream)))
+    return cuda_fail(c, e, "check word");
   if ((e = cudaStreamSynchronize(c->stream))) return cuda_fail(c, e, "join");
+  if (check & kErrBounds) return set_error(c, KNNG_E_BOUNDS, "join: an id outside [0, n) (bounds check)");
   if (updates) *updates = int64_t(h);
   return KNNG_OK;
 }
@@ -878,9 +901,21 @@ int knng_export(const int32_t* ids_dev, const int32_t* scores_dev, int64_t n, in
                 const int32_t* id_map_dev, int32_t* knns_dev, float* dists_dev, void* stream) {
   if (!ids_dev || !scores_dev || !knns_dev || !dists_dev || n < 0 || k_eval < 1 || k_eval > k_build)
     return KNNG_E_ARGS;
-  cudaError_t e = launch_export(ids_dev, scores_dev, n, k_build, k_eval, id_map_dev, knns_dev, dists_dev,
-                                static_cast<cudaStream_t>(stream));
-  return e ? KNNG_E_CUDA : KNNG_OK;
+  const cudaStream_t str = static_cast<cudaStream_t>(stream);
+  unsigned* word = nullptr;
+  if (kChecked && (export_check_word(&word) != cudaSuccess || cudaMemsetAsync(word, 0, sizeof(unsigned), str)))
+    return KNNG_E_CUDA;
+  cudaError_t e = launch_export(ids_dev, scores_dev, n, k_build, k_eval, id_map_dev, knns_dev, dists_dev, str,
+                                nullptr, word);
+  if (e) return KNNG_E_CUDA;
+  if (kChecked) {  // the bounds-checked build waits for the stage to read its error word
+    unsigned check = 0;
+    if (cudaMemcpyAsync(&check, word, sizeof(unsigned), cudaMemcpyDeviceToHost, str) ||
+        cudaStreamSynchronize(str))
+      return KNNG_E_CUDA;
+    if (check & kErrBounds) return KNNG_E_BOUNDS;
+  }
+  return KNNG_OK;
 }
 
 int knng_build(knng_ctx* c, const void* rows, int64_t n, int d, int rows_on_device, int32_t* knns, float* dists,

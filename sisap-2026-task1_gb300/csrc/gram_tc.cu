@@ -119,7 +119,9 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
                                                                       const int32_t* __restrict__ leaf_start,
                                                                       int64_t nleaves, int64_t total,
                                                                       int32_t* __restrict__ gram, int64_t gram_pos0,
-                                                                      unsigned* err, long long spin_limit) {
+                                                                      unsigned* err, long long spin_limit,
+                                                                      int64_t n_rows) {
+  (void)n_rows;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
@@ -186,7 +188,12 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
         const int idx = tid + kTcThreads * u;  // 512 pieces of 16 bytes: row idx / 4, piece idx % 4
         const int r = idx >> 2, pc = idx & 3;
         const int32_t id = row_id[b][r];
-        if (id >= 0) cp_async16(dst + ring_offset(r, pc), codes + int64_t(id) * d + ic * kChunk + pc * 16);
+        // (bounds-checked build) -1 marks a row past its leaf's end; any other
+        // id must be a row of `codes`
+        if (id >= 0 && KNNG_GUARD(err, id < n_rows))
+          cp_async16(dst + ring_offset(r, pc), codes + int64_t(id) * d + ic * kChunk + pc * 16);
+        else
+          KNNG_FLAG_IF(err, id < -1);
       }
       if (++ic == nchunks) {
         ic = 0;
@@ -353,7 +360,7 @@ __global__ void __launch_bounds__(kTcThreads, kCtasPerSm) leaf_gram_tc(const int
 
 cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm, const int32_t* leaf_start,
                                 int64_t nleaves, int64_t total, int32_t* gram, int64_t gram_pos0, unsigned* err,
-                                int num_sms, cudaStream_t s, int wait_limit) {
+                                int num_sms, cudaStream_t s, int wait_limit, int64_t n_rows) {
   if (d % kChunk != 0) return cudaErrorInvalidValue;
   const size_t smem = 2 * size_t(kStageBytes) + size_t(kRing) * kI8Bytes + 1024;  // + alignment slack
   KNNG_CUDA_TRY(ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram_tc), smem));
@@ -366,7 +373,7 @@ cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm,
   // main loop gives up at once (the drain keeps the full limit)
   const long long spins = wait_limit > 0 ? (long long)wait_limit : wait_limit < 0 ? 0ll : kSpinLimit;
   leaf_gram_tc<<<unsigned(blocks), kTcThreads, smem, s>>>(codes, d, perm, leaf_start, nleaves, total, gram, gram_pos0,
-                                                          err, spins);
+                                                          err, spins, n_rows);
   note_launch();
   return cudaGetLastError();
 }

@@ -38,15 +38,19 @@ __global__ void leaf_starts(const uint8_t* __restrict__ f, const int32_t* __rest
 // per position: inverse permutation, leaf start and leaf size
 __global__ void leaf_fill(const int32_t* __restrict__ leaf_start, int64_t nleaves, int64_t total, int64_t n,
                           const int32_t* __restrict__ perm, int32_t* __restrict__ pos, int32_t* __restrict__ leaf_lo,
-                          uint8_t* __restrict__ leaf_sz) {
+                          uint8_t* __restrict__ leaf_sz, unsigned* err) {
+  (void)err;
   for (int64_t l = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; l < nleaves; l += int64_t(gridDim.x) * blockDim.x) {
     const int64_t s = leaf_start[l];
     const int64_t e = l + 1 < nleaves ? leaf_start[l + 1] : total;
     const int64_t tb = (s / n) * n;
+    // a leaf holds 1..kMaxLeaf positions of one tree
+    KNNG_FLAG_IF(err, e - s < 1 || e - s > kMaxLeaf || e > tb + n);
     for (int64_t p = s; p < e; ++p) {
       leaf_lo[p] = int32_t(s);
       leaf_sz[p] = uint8_t(e - s);
-      pos[tb + perm[p]] = int32_t(p);
+      const int32_t v = perm[p];
+      if (KNNG_GUARD(err, v >= 0 && v < n)) pos[tb + v] = int32_t(p);
     }
   }
 }
@@ -62,7 +66,10 @@ __global__ void __launch_bounds__(kGramThreads) leaf_gram(const int8_t* __restri
                                                           const int32_t* __restrict__ perm,
                                                           const int32_t* __restrict__ leaf_start,
                                                           int64_t nleaves, int64_t total,
-                                                          int32_t* __restrict__ gram, int64_t gram_pos0) {
+                                                          int32_t* __restrict__ gram, int64_t gram_pos0,
+                                                          int64_t n_rows, unsigned* err) {
+  (void)n_rows;
+  (void)err;
   extern __shared__ uint4 rows_s[];
   const int stride16 = d / 16 + 1;  // in uint4
   for (int64_t l = blockIdx.x; l < nleaves; l += gridDim.x) {
@@ -74,7 +81,10 @@ __global__ void __launch_bounds__(kGramThreads) leaf_gram(const int8_t* __restri
     for (int c = threadIdx.x; c < kMaxLeaf * nchunk; c += kGramThreads) {
       const int r = c / nchunk, cc = c % nchunk;
       uint4 v = make_uint4(0, 0, 0, 0);
-      if (r < m) v = __ldg(reinterpret_cast<const uint4*>(codes + int64_t(perm[s + r]) * d) + cc);
+      if (r < m) {
+        const int32_t id = perm[s + r];
+        if (KNNG_GUARD(err, id >= 0 && id < n_rows)) v = __ldg(reinterpret_cast<const uint4*>(codes + int64_t(id) * d) + cc);
+      }
       rows_s[r * stride16 + cc] = v;
     }
     __syncthreads();
@@ -153,7 +163,10 @@ __global__ void __launch_bounds__(256) init_merge(int64_t n, int t0, int t1, int
                                                   const uint8_t* __restrict__ leaf_sz,
                                                   const int32_t* __restrict__ gram, int64_t gram_pos0,
                                                   int32_t* __restrict__ ids, int32_t* __restrict__ scores,
-                                                  int32_t* __restrict__ fix_rows, int64_t* __restrict__ fix_count) {
+                                                  int32_t* __restrict__ fix_rows, int64_t* __restrict__ fix_count,
+                                                  int64_t gram_rows, unsigned* err) {
+  (void)gram_rows;
+  (void)err;
   const int lane = threadIdx.x & 31;
   const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
   for (int64_t i = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
@@ -171,8 +184,12 @@ __global__ void __launch_bounds__(256) init_merge(int64_t n, int t0, int t1, int
     }
     for (int t = t0; t < t1; ++t) {
       const int64_t p = pos[int64_t(t) * n + i];
+      // (bounds-checked build) the position lies in tree t, its leaf in the
+      // same tree, and its Gram row in this chunk's rows
+      if (!KNNG_GUARD(err, p >= int64_t(t) * n && p < int64_t(t + 1) * n && p - gram_pos0 < gram_rows)) continue;
       const int64_t s = leaf_lo[p];
       const int m = leaf_sz[p];
+      if (!KNNG_GUARD(err, s >= int64_t(t) * n && s <= p && s + m <= int64_t(t + 1) * n && p < s + m)) continue;
       const int self = int(p - s);
       const int32_t* grow = gram + (p - gram_pos0) * int64_t(kMaxLeaf);
 #pragma unroll
@@ -475,14 +492,16 @@ __global__ void __launch_bounds__(256) init_block_kernel(const int8_t* __restric
 
 __global__ void export_kernel(const int32_t* __restrict__ ids, const int32_t* __restrict__ scores, int64_t n,
                               int K, int k_eval, const int32_t* __restrict__ id_map, int32_t* __restrict__ knns,
-                              float* __restrict__ dists, JobTable jt) {
+                              float* __restrict__ dists, JobTable jt, unsigned* err) {
+  (void)err;
   const int64_t tot = n * k_eval;
   for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < tot; q += int64_t(gridDim.x) * blockDim.x) {
     const int64_t i = q / k_eval;
     const int k = int(q % k_eval);
     int32_t id = ids[i * K + k];
     const int32_t sc = scores[i * K + k];
-    if (id_map) id = id_map[id];
+    if (id_map && KNNG_GUARD(err, id >= 0 && id < n)) id = id_map[id];
+    else KNNG_FLAG_IF(err, id < 0 || id >= n);
     if (jt.count > 1) id -= jt.off[job_of(jt, i)];
     const int64_t o = i * k_eval + (k_eval - 1 - k);
     knns[o] = id + 1;
@@ -537,12 +556,15 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
   if ((e = cudaStreamSynchronize(s))) return fail(e, "leaf table");
   lt[T] = int32_t(nleaves);
   if (leaves_out) *leaves_out = nleaves;
+  // error word of the tensor-core Gram's bounded waits and of the
+  // bounds-checked build's checks
+  unsigned* gerr = reinterpret_cast<unsigned*>(ib.dev_i64 + 3);
+  const bool read_err = gram_mode == 1 || kChecked;
+  if (read_err && (e = cudaMemsetAsync(gerr, 0, sizeof(unsigned), s))) return fail(e, "error word");
   cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   leaf_fill<<<unsigned(std::min<int64_t>(grid1(nleaves), int64_t(sms) * 32)), 256, 0, s>>>(
-      leaf_start, nleaves, tn, n, perm, ib.pos, ib.leaf_lo, ib.leaf_sz);
+      leaf_start, nleaves, tn, n, perm, ib.pos, ib.leaf_lo, ib.leaf_sz, gerr);
   note_launch();
-  unsigned* gerr = reinterpret_cast<unsigned*>(ib.dev_i64 + 3);
-  if (gram_mode == 1 && (e = cudaMemsetAsync(gerr, 0, sizeof(unsigned), s))) return fail(e, "gram flag");
   if ((e = cudaMemsetAsync(ib.dev_i64 + 1, 0, 8, s))) return fail(e, "fix count");
   const size_t gram_smem = size_t(kMaxLeaf) * (d / 16 + 1) * 16;
   if (gram_mode != 1 && (e = ensure_smem_attr(reinterpret_cast<const void*>(leaf_gram), gram_smem)))
@@ -559,30 +581,34 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
     if (l1 > l0) {
       if (gram_mode == 1) {
         if ((e = launch_leaf_gram_tc(codes, d, perm, leaf_start + l0, l1 - l0, pos1, ib.gram, pos0, gerr, sms, s,
-                                     wait_limit)))
+                                     wait_limit, n)))
           return fail(e, "tensor-core gram");
       } else {
         cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
         leaf_gram<<<unsigned(std::min<int64_t>(l1 - l0, int64_t(sms) * 24)), kGramThreads, gram_smem, s>>>(
-            codes, d, perm, leaf_start + l0, l1 - l0, pos1, ib.gram, pos0);
+            codes, d, perm, leaf_start + l0, l1 - l0, pos1, ib.gram, pos0, n, gerr);
         note_launch();
       }
     }
     cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
     init_merge<<<unsigned(std::min<int64_t>((n + 7) / 8, int64_t(sms) * 16)), 256, 0, s>>>(
         n, t0, t1, K, t0 == 0 ? 1 : 0, t1 == T ? 1 : 0, perm, ib.pos, ib.leaf_lo, ib.leaf_sz, ib.gram, pos0, ids,
-        scores, ib.fix_rows, ib.dev_i64 + 1);
+        scores, ib.fix_rows, ib.dev_i64 + 1, int64_t(t1 - t0) * n, gerr);
     note_launch();
   }
   int64_t nfix = 0;
   unsigned gflag = 0;
   if ((e = cudaMemcpyAsync(&nfix, ib.dev_i64 + 1, 8, cudaMemcpyDeviceToHost, s))) return fail(e, "fix count");
-  if (gram_mode == 1 && (e = cudaMemcpyAsync(&gflag, gerr, sizeof(unsigned), cudaMemcpyDeviceToHost, s)))
-    return fail(e, "gram flag");
+  if (read_err && (e = cudaMemcpyAsync(&gflag, gerr, sizeof(unsigned), cudaMemcpyDeviceToHost, s)))
+    return fail(e, "error word");
   if ((e = cudaStreamSynchronize(s))) return fail(e, "init merge");
   if (gflag & kErrTimeout) {
     if (err) *err = "tensor-core leaf Gram: an mbarrier wait timed out";
     return KNNG_E_TIMEOUT;
+  }
+  if (gflag & kErrBounds) {
+    if (err) *err = "initial graph: a permutation entry or leaf position is outside its array (bounds check)";
+    return KNNG_E_BOUNDS;
   }
   if (nfix > 0) {
     cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
@@ -613,15 +639,24 @@ cudaError_t launch_init_block(const int8_t* codes, int d, int64_t n_total, int K
 }
 
 cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, int K, int k_eval,
-                          const int32_t* id_map, int32_t* knns, float* dists, cudaStream_t s, const JobTable* jt) {
+                          const int32_t* id_map, int32_t* knns, float* dists, cudaStream_t s, const JobTable* jt,
+                          unsigned* err) {
   const int64_t tot = n * k_eval;
   if (tot <= 0) return cudaSuccess;
   const JobTable none{};
   cudaGetLastError();  // clear a stale, non-sticky error: the launch reports only its own
   export_kernel<<<unsigned(std::min<int64_t>(grid1(tot), 4096)), 256, 0, s>>>(ids, scores, n, K, k_eval, id_map,
-                                                                               knns, dists, jt ? *jt : none);
+                                                                               knns, dists, jt ? *jt : none, err);
   note_launch();
   return cudaGetLastError();
+}
+
+// The bounds-checked build's error word for knng_export (a stage entry point
+// without a context).  Host code reaches it only through its device address.
+__device__ unsigned g_export_check;
+
+cudaError_t export_check_word(unsigned** word) {
+  return cudaGetSymbolAddress(reinterpret_cast<void**>(word), g_export_check);
 }
 
 }  // namespace knng

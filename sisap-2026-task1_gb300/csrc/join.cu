@@ -225,6 +225,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
   for (int64_t r = blockIdx.x; r < nrows; r += gridDim.x) {
     const int64_t i = next_i;
     if (r + gridDim.x < nrows) next_i = row_order ? int64_t(row_order[r + gridDim.x]) : r + gridDim.x;
+    if (!KNNG_GUARD(ctl.check_err, i >= 0 && i < n)) continue;  // block-uniform
     int job = 0;
     if (ctl.job_done) {
       job = job_of(jt, i);
@@ -251,6 +252,7 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
       const int32_t id = ids_in[i * K + k];
       pool_id[k] = id;
       pool_sc[k] = scores_in[i * K + k];
+      KNNG_FLAG_IF(ctl.check_err, id < 0 || id >= n);
       if (ctl.chg_in) moved |= (id < 0 || id >= n) ? 1 : int(ctl.chg_in[id]);
     }
     if (ctl.chg_in && tid == 0) moved |= int(ctl.chg_in[i]);
@@ -318,7 +320,10 @@ __global__ void __launch_bounds__(kThreads, MINB) join_kernel(
         if (j < KK) {
           const int k = int((uint32_t(j) * kdiv) >> 20);
           const int32_t n1 = pool_id[k];
-          if (n1 >= 0 && n1 < n) val = ids_in[int64_t(n1) * K + (j - k * K)];
+          if (n1 >= 0 && n1 < n) {
+            val = ids_in[int64_t(n1) * K + (j - k * K)];
+            KNNG_FLAG_IF(ctl.check_err, val < 0 || val >= n);
+          }
         }
         v[t] = val;
       }

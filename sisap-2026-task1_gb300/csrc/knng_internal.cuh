@@ -18,6 +18,29 @@ constexpr int kScoreMinI = INT32_MIN;
 // Device-side error flag bits (written by kernels, read by the host).
 enum : unsigned { kErrReplay = 1u, kErrBounds = 2u, kErrTimeout = 4u };
 
+// Bounds-checked build (compiled with -DKNNG_CHECKS into libknng_checked.so).
+// Every index a kernel derives from its inputs before it addresses memory
+// (graph ids, permutation entries, leaf positions, id maps) is checked; a
+// failed check ORs kErrBounds into the call's error word and the access is
+// skipped or replaced by a harmless one, so a bad input ends in
+// KNNG_E_BOUNDS, never in a fault or a trap.  In the default build
+// KNNG_GUARD(err, ok) is `true` (no check is compiled) and KNNG_FLAG_IF
+// compiles to nothing; guards that the default build needs for its own
+// correctness are written out in full either way.
+#ifdef KNNG_CHECKS
+constexpr bool kChecked = true;
+__device__ __forceinline__ bool check_note(unsigned* err, bool ok) {
+  if (!ok && err) atomicOr(err, kErrBounds);
+  return ok;
+}
+#define KNNG_GUARD(err, ok) (::knng::check_note((err), bool(ok)))
+#define KNNG_FLAG_IF(err, bad) ((void)::knng::check_note((err), !(bad)))
+#else
+constexpr bool kChecked = false;
+#define KNNG_GUARD(err, ok) true
+#define KNNG_FLAG_IF(err, bad) ((void)0)
+#endif
+
 inline bool dim_ok(int d) { return d >= 128 && d <= kMaxDim && d % 128 == 0; }
 
 // Host-side count of kernels this library has launched (all contexts).
@@ -127,7 +150,8 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
 // at position `total`) go to gram[(position - gram_pos0) * 64 ...].
 cudaError_t launch_leaf_gram_tc(const int8_t* codes, int d, const int32_t* perm, const int32_t* leaf_start,
                                 int64_t nleaves, int64_t total, int32_t* gram, int64_t gram_pos0, unsigned* err,
-                                int num_sms, cudaStream_t s, int wait_limit = 0);
+                                int num_sms, cudaStream_t s, int wait_limit, int64_t n_rows);
+// n_rows: rows of `codes` (the bounds-checked build checks every gathered id against it)
 
 // Random initial graph (init_mode KNNG_INIT_RANDOM); every job needs n > K.
 cudaError_t launch_init_random(const int8_t* codes, int d, int64_t n_total, int K, uint32_t seed, const JobTable& jt,
@@ -164,6 +188,9 @@ struct JoinCtl {
   // before the first); the launch writes this iteration's flags to chg_out.
   const uint8_t* chg_in;
   uint8_t* chg_out;
+  // error word of the bounds-checked build (null: none): an id outside [0, n)
+  // in the input lists or the row order sets kErrBounds
+  unsigned* check_err;
 };
 // Entries per row of the candidate cache (rows with more distinct candidates
 // keep the first ones; the rest are scored again) and its bytes for n rows.
@@ -199,8 +226,12 @@ const char* join_variant_error();                    // detail of the last faile
 // ---- export (init.cu) ----
 cudaError_t launch_export(const int32_t* ids, const int32_t* scores, int64_t n, int K, int k_eval,
                           const int32_t* id_map, int32_t* knns, float* dists, cudaStream_t s,
-                          const JobTable* jt = nullptr);
-// With jt, ids are written job-local (id - off[job] + 1).
+                          const JobTable* jt = nullptr, unsigned* err = nullptr);
+// With jt, ids are written job-local (id - off[job] + 1).  err: the
+// bounds-checked build's error word (an id outside [0, n)), may be null.
+// The bounds-checked build's error word of knng_export, which has no context:
+// a file-scope device word of init.cu, resolved once per device.
+cudaError_t export_check_word(unsigned** word);
 
 }  // namespace knng
 

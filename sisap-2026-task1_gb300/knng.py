@@ -15,7 +15,9 @@ import os
 import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libknng.so")
+# KNNG_LIBRARY selects another build of the library, e.g. the bounds-checked
+# libknng_checked.so (build.py --checked)
+LIB_PATH = os.environ.get("KNNG_LIBRARY") or os.path.join(PKG, "libknng.so")
 
 QUANT_TRUNC, QUANT_ROUND = 0, 1
 JOIN_JACOBI, JOIN_INPLACE = 0, 1
@@ -25,7 +27,7 @@ INIT_FOREST, INIT_RANDOM, INIT_BLOCK = 0, 1, 2
 SKETCH_SIGN, SKETCH_HYPERPLANE = 0, 1
 
 STATUS = {0: "ok", -1: "E_ARGS", -2: "E_DIM", -3: "E_OOM", -4: "E_ADMIT", -5: "E_TIMEOUT", -6: "E_CUDA",
-          -7: "E_REPLAY", -8: "E_BUSY", -9: "E_NOTFOUND", -10: "E_SCRATCH"}
+          -7: "E_REPLAY", -8: "E_BUSY", -9: "E_NOTFOUND", -10: "E_SCRATCH", -11: "E_BOUNDS"}
 
 
 class KnngError(RuntimeError):
@@ -79,7 +81,8 @@ def lib():
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise RuntimeError(f"libknng.so not found at {LIB_PATH}: run __graft_entry__.build() first")
+            raise RuntimeError(f"{os.path.basename(LIB_PATH)} not found at {LIB_PATH}: run __graft_entry__.build() "
+                               "first")
         L = C.CDLL(LIB_PATH)
         P, V, I64 = C.POINTER, C.c_void_p, C.c_int64
         L.knng_default_params.argtypes = [P(Params)]
