@@ -160,11 +160,13 @@ void knng_destroy(knng_ctx* ctx);
 
 /* Build the all-points kNN graph of n rows of d float32 (row-major).
  * Replaces src/main.cpp:179-457 (quantise, forest, init, NN-Descent, export).
- * rows      : host or device pointer (rows_on_device selects).  Host rows are
- *             read in place by the quantise kernel when the device can reach
- *             them (mapped pinned memory, or pageable memory on devices with
- *             coherent pageable access such as Grace + NVLink-C2C); otherwise
- *             they are copied through device staging buffers.
+ * rows      : host or device pointer (rows_on_device selects).  Host rows in
+ *             memory the device maps (pinned, registered or managed) are read
+ *             in place by the quantise kernel over the host link; pageable
+ *             rows (malloc, std::vector, numpy) are copied by host threads
+ *             through pinned buffers of the context, and the device never
+ *             touches the pageable memory itself.  Host knns/dists in
+ *             pageable memory are written the same way.
  * knns      : n * k_eval int32, 1-based ids, each row worst -> best
  *             (src/main.cpp:452, 455).
  * dists     : n * k_eval float32 int8 inner products, same order (:453, 456).
@@ -225,11 +227,12 @@ int knng_release(knng_server* sv, uint64_t ticket);
 void knng_server_destroy(knng_server* sv);
 
 /* Device bytes a build of n rows of dimension d needs with parameters p
- * (NULL = defaults): the admission estimate of the serving loop. */
+ * (NULL = defaults): the admission estimate of the serving loop.  Host rows
+ * need no device staging (rows_on_device does not change the figure). */
 int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on_device);
 
 /* Return all of the context's device buffers to the stream-ordered pool
- * (kept for reuse otherwise). */
+ * and free its pinned host staging buffers (kept for reuse otherwise). */
 int knng_trim(knng_ctx* ctx);
 
 /* Text for a status code, and the last detailed error message of ctx. */

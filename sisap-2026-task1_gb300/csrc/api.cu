@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -98,11 +99,17 @@ struct knng_ctx {
   cudaEvent_t ev[8] = {};
   cudaEvent_t jev[2] = {};
   cudaEvent_t bev = nullptr;  // start of a batch (all dimension groups wait on it)
-  cudaStream_t copy_stream = nullptr;  // host-input chunks, overlapped with quantisation
-  cudaEvent_t copied[2] = {}, freed[2] = {};
+  cudaEvent_t freed[2] = {};  // pinned input slot s is free again once freed[s] completes
+  // pageable caller memory goes through these pinned buffers, copied by host threads
+  PinnedBuf pin_in, pin_out;
+  std::unique_ptr<CopyPool> pool;
+  CopyPool& copier() {
+    if (!pool) pool.reset(new CopyPool(host_copy_threads()));
+    return *pool;
+  }
   cudaEvent_t itev[kMaxIterEvents] = {};
   std::string last_error;
-  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, staging, outbuf, scalars, jobs, hsketch, rowflags;
+  DevBuf codes, sketch, graph, perm, leaf_flag, scratch, outbuf, scalars, jobs, hsketch, rowflags;
   // join phase captured as a CUDA graph, reused while the launch key matches
   cudaGraphExec_t join_graph = nullptr;
   std::vector<uintptr_t> join_graph_key;
@@ -111,8 +118,7 @@ struct knng_ctx {
   std::map<std::pair<int, int>, JoinCfg> tuned;
   std::vector<knng_ctx*> subs;  // contexts of the second and later dimension groups of a batch
   std::vector<DevBuf*> buffers() {
-    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &staging, &outbuf, &scalars, &jobs, &hsketch,
-            &rowflags};
+    return {&codes, &sketch, &graph, &perm, &leaf_flag, &scratch, &outbuf, &scalars, &jobs, &hsketch, &rowflags};
   }
   // the sketches the join scores and their 64-bit words per row
   bool hyperplane() const { return prm.sketch_mode == KNNG_SKETCH_HYPERPLANE; }
@@ -269,43 +275,40 @@ int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_devic
     e = launch_quantize(static_cast<const float*>(rows), n, d, c->prm.quant_mode, codes, sketch, c->stream);
     return e ? cuda_fail(c, e, "quantize") : KNNG_OK;
   }
-  // Host rows the device can read itself -- mapped pinned memory, or any
-  // pageable memory when the device accesses it coherently through the host
-  // page tables (Grace + NVLink-C2C) -- are quantised straight from host
-  // memory by one kernel: no staging copies, at the link's read bandwidth.
+  // Host rows in memory the device maps (pinned or registered host memory,
+  // managed memory) are quantised in place by one kernel over the host link.
   {
     cudaPointerAttributes at{};
     const float* direct = nullptr;
     if (cudaPointerGetAttributes(&at, rows) == cudaSuccess) {
-      if (at.type == cudaMemoryTypeHost && at.devicePointer) direct = static_cast<const float*>(at.devicePointer);
-      else if (at.type == cudaMemoryTypeUnregistered && c->pageable_access) direct = static_cast<const float*>(rows);
+      if ((at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeManaged) && at.devicePointer)
+        direct = static_cast<const float*>(at.devicePointer);
     } else {
-      cudaGetLastError();  // an unknown pointer takes the staging path
+      cudaGetLastError();  // an unknown pointer is pageable memory
     }
     if (direct) {
       e = launch_quantize(direct, n, d, c->prm.quant_mode, codes, sketch, c->stream);
       return e ? cuda_fail(c, e, "quantize (host rows)") : KNNG_OK;
     }
   }
-  // Otherwise stream fixed-size chunks through two staging buffers; the copy
-  // of chunk k+1 (copy stream) overlaps the quantisation of chunk k (context
-  // stream), ordered by per-buffer events (the reference streams 2.2M-row
-  // hyperslabs the same way, src/main.cpp:165-177).
+  // Pageable rows: host threads copy fixed-size chunks into two pinned slots
+  // and the kernel quantises each slot in place while the threads fill the
+  // other (hostcopy.cu says why the device never reads pageable memory).
+  // Slot s is refilled once the kernel that read it (event freed[s]) is done.
   const int64_t chunk_rows = std::min<int64_t>(kStageRows, n);
   const size_t chunk_bytes = size_t(chunk_rows) * d * 4;
-  if ((e = c->staging.ensure(2 * chunk_bytes))) return cuda_fail(c, e, "staging allocation");
+  if ((e = c->pin_in.ensure(2 * chunk_bytes))) return cuda_fail(c, e, "pinned input staging");
+  float* slot_dev[2];
+  for (int b = 0; b < 2; ++b)
+    if ((e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&slot_dev[b]), c->pin_in.as<char>(b * chunk_bytes), 0)))
+      return cuda_fail(c, e, "pinned input staging");
   const float* src = static_cast<const float*>(rows);
-  if ((e = cudaEventRecord(c->freed[0], c->stream)) || (e = cudaEventRecord(c->freed[1], c->stream)))
-    return cuda_fail(c, e, "staging events");
   for (int64_t off = 0, k = 0; off < n; off += chunk_rows, ++k) {
     const int64_t m = std::min<int64_t>(chunk_rows, n - off);
     const int b = int(k & 1);
-    float* stage = c->staging.as<float>(b * chunk_bytes);
-    if ((e = cudaStreamWaitEvent(c->copy_stream, c->freed[b], 0)) ||
-        (e = cudaMemcpyAsync(stage, src + off * d, size_t(m) * d * 4, cudaMemcpyHostToDevice, c->copy_stream)) ||
-        (e = cudaEventRecord(c->copied[b], c->copy_stream)) || (e = cudaStreamWaitEvent(c->stream, c->copied[b], 0)))
-      return cuda_fail(c, e, "input copy");
-    if ((e = launch_quantize(stage, m, d, c->prm.quant_mode, codes + off * d, sketch + off * W, c->stream)))
+    if ((e = cudaEventSynchronize(c->freed[b]))) return cuda_fail(c, e, "input staging");
+    c->copier().copy(c->pin_in.as<char>(b * chunk_bytes), src + off * d, size_t(m) * d * 4);
+    if ((e = launch_quantize(slot_dev[b], m, d, c->prm.quant_mode, codes + off * d, sketch + off * W, c->stream)))
       return cuda_fail(c, e, "quantize");
     if ((e = cudaEventRecord(c->freed[b], c->stream))) return cuda_fail(c, e, "staging events");
   }
@@ -625,12 +628,22 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   }
   if ((e = launch_export(ids[fin], scs[fin], N, K, p.k_eval, nullptr, kd, dd, str, &jt, ctl.check_err)))
     return cuda_fail(c, e, "export");
+  // pageable host outputs: copied into pinned memory here and by host threads
+  // into the caller's buffers after the stream is done (hostcopy.cu)
+  std::vector<char> via_pin(jb, 0);
+  bool any_pin = false;
+  for (int b = 0; b < J; ++b)
+    if (!direct && !jobs[b].out_dev && (host_pageable(jobs[b].knns) || host_pageable(jobs[b].dists)))
+      any_pin = (via_pin[b] = 1);
+  if (any_pin && (e = c->pin_out.ensure(outn * 8))) return cuda_fail(c, e, "pinned output staging");
   if (!direct)
     for (int b = 0; b < J; ++b) {
       const size_t cnt_b = size_t(jobs[b].n) * p.k_eval, at = size_t(hoff[b]) * p.k_eval;
       const cudaMemcpyKind kind = jobs[b].out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-      if ((e = cudaMemcpyAsync(jobs[b].knns, kd + at, cnt_b * 4, kind, str)) ||
-          (e = cudaMemcpyAsync(jobs[b].dists, dd + at, cnt_b * 4, kind, str)))
+      int32_t* ko = via_pin[b] ? c->pin_out.as<int32_t>(at * 4) : jobs[b].knns;
+      float* dso = via_pin[b] ? c->pin_out.as<float>((outn + at) * 4) : jobs[b].dists;
+      if ((e = cudaMemcpyAsync(ko, kd + at, cnt_b * 4, kind, str)) ||
+          (e = cudaMemcpyAsync(dso, dd + at, cnt_b * 4, kind, str)))
         return cuda_fail(c, e, "output copy");
     }
   cudaEventRecord(c->ev[5], str);
@@ -640,6 +653,12 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   if ((e = cudaStreamSynchronize(str))) return cuda_fail(c, e, "build");
   if (check & kErrBounds)
     return set_error(c, KNNG_E_BOUNDS, "NN-Descent or export: an id outside [0, n) (bounds check)");
+  for (int b = 0; b < J; ++b)
+    if (via_pin[b]) {
+      const size_t cnt_b = size_t(jobs[b].n) * p.k_eval, at = size_t(hoff[b]) * p.k_eval;
+      c->copier().copy(jobs[b].knns, c->pin_out.as<int32_t>(at * 4), cnt_b * 4);
+      c->copier().copy(jobs[b].dists, c->pin_out.as<float>((outn + at) * 4), cnt_b * 4);
+    }
   int max_it = 0;
   for (int b = 0; b < J; ++b) {
     jobs[b].iterations = iters[b];
@@ -761,13 +780,12 @@ int knng_create(knng_ctx** out, const knng_params* p) {
       knng_destroy(c);
       return KNNG_E_CUDA;
     }
-  if ((e = cudaEventCreate(&c->bev)) || (e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking))) {
+  if ((e = cudaEventCreate(&c->bev))) {
     knng_destroy(c);
     return KNNG_E_CUDA;
   }
   for (int k = 0; k < 2; ++k)
-    if ((e = cudaEventCreateWithFlags(&c->copied[k], cudaEventDisableTiming)) ||
-        (e = cudaEventCreateWithFlags(&c->freed[k], cudaEventDisableTiming))) {
+    if ((e = cudaEventCreateWithFlags(&c->freed[k], cudaEventDisableTiming))) {
       knng_destroy(c);
       return KNNG_E_CUDA;
     }
@@ -793,11 +811,11 @@ void knng_destroy(knng_ctx* c) {
   for (auto& ev : c->itev)
     if (ev) cudaEventDestroy(ev);
   if (c->bev) cudaEventDestroy(c->bev);
-  for (int k = 0; k < 2; ++k) {
-    if (c->copied[k]) cudaEventDestroy(c->copied[k]);
+  for (int k = 0; k < 2; ++k)
     if (c->freed[k]) cudaEventDestroy(c->freed[k]);
-  }
-  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  c->pool.reset();
+  c->pin_in.release();
+  c->pin_out.release();
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : c->jev)
@@ -947,7 +965,7 @@ int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on
   if (q.join_mode == KNNG_JOIN_JACOBI) b += size_t(2) * n;          // row-change flags
 
   if (q.sketch_mode == KNNG_SKETCH_HYPERPLANE) b += size_t(n) * 16;  // hyperplane sketches
-  if (!rows_on_device) b += size_t(2) * std::min<int64_t>(kStageRows, n) * d * 4;  // host-input staging
+  (void)rows_on_device;  // host rows are staged through pinned host memory, not device memory
   return int64_t(b) + (int64_t(1) << 24);                          // pool rounding slack
 }
 
@@ -960,6 +978,9 @@ int knng_trim(knng_ctx* c) {
     c->join_graph_key.clear();
   }
   for (DevBuf* b : c->buffers()) b->release();
+  cudaStreamSynchronize(c->stream);  // no copy still reads or writes the pinned buffers
+  c->pin_in.release();
+  c->pin_out.release();
   for (knng_ctx* sub : c->subs) knng_trim(sub);
   return KNNG_OK;
 }

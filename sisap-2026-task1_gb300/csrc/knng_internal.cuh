@@ -2,9 +2,13 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <condition_variable>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "../../include/knng.h"
 
@@ -73,6 +77,43 @@ __device__ __forceinline__ int job_of(const JobTable& jt, int64_t row) {
   }
   return lo;
 }
+
+// ---- hostcopy.cu ----
+// Pinned host memory (cudaHostAlloc), grown on demand.
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t want);
+  void release();
+  template <class T>
+  T* as(size_t byte_off = 0) const {
+    return reinterpret_cast<T*>(static_cast<char*>(p) + byte_off);
+  }
+};
+// Host threads that split one large memcpy between them (the caller takes a
+// slice too); copy() returns when every slice is done.  One copy at a time.
+class CopyPool {
+ public:
+  explicit CopyPool(int threads);
+  ~CopyPool();
+  void copy(void* dst, const void* src, size_t bytes);
+
+ private:
+  void run(int t);
+  void slice(int t);
+  int nthreads_;
+  std::vector<std::thread> workers_;
+  std::mutex mu_;
+  std::condition_variable start_cv_, done_cv_;
+  uint64_t gen_ = 0;
+  int pending_ = 0;
+  bool stop_ = false;
+  char* dst_ = nullptr;
+  const char* src_ = nullptr;
+  size_t bytes_ = 0;
+};
+int host_copy_threads();            // CPUs this process may run on (1..32)
+bool host_pageable(const void* p);  // host memory the device does not map
 
 // ---- quantize.cu ----
 cudaError_t launch_quantize(const float* x, int64_t n, int d, int quant_mode, int8_t* codes,
