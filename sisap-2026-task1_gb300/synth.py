@@ -10,7 +10,11 @@ available offline, so every workload is synthetic with its shape:
 All arithmetic is float64 numpy with a PCG64 generator, then cast to float32,
 so the same (n, d, centres, seed) gives the same bytes on every host.
 ``mixture_torch`` draws the same kind of data on a CUDA device for sizes that
-numpy would take minutes over (it is a different stream of random numbers).
+numpy would take minutes over (it is a different stream of random numbers): the
+cluster labels come from numpy's PCG64 on the host and the centres and noise
+from torch's seeded CUDA generator, so the same arguments give the same bytes in
+every process on the same GPU type (torch.multinomial over tens of thousands of
+categories on CUDA did not: its rows differed from process to process).
 """
 from __future__ import annotations
 
@@ -49,12 +53,12 @@ def mixture_torch(n: int, d: int, centres: int, seed: int, device="cuda", chunk:
     g.manual_seed(seed)
     c = torch.randn(centres, d, generator=g, device=device, dtype=torch.float32)
     c /= c.norm(dim=1, keepdim=True)
-    w = torch.as_tensor(zipf_weights(centres), device=device, dtype=torch.float32)
+    labels = np.random.Generator(np.random.PCG64(seed)).choice(centres, size=n, p=zipf_weights(centres))
     out = torch.empty(n, d, device=device, dtype=torch.float32)
     sigma = NOISE / d ** 0.5
     for s in range(0, n, chunk):
         e = min(n, s + chunk)
-        lab = torch.multinomial(w, e - s, replacement=True, generator=g)
+        lab = torch.from_numpy(labels[s:e]).to(device)
         x = c[lab] + sigma * torch.randn(e - s, d, generator=g, device=device)
         out[s:e] = x / x.norm(dim=1, keepdim=True)
     return out
