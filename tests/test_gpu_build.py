@@ -112,6 +112,37 @@ def test_build_is_deterministic_and_io_independent(knng_mod):
     np.testing.assert_array_equal(d1, d3.cpu().numpy())
 
 
+CHILD_BUILD = """
+import hashlib, sys
+sys.path[:0] = [{pkg!r}]
+import knng, synth, torch
+x = synth.mixture_torch(400_000, 1024, 4_000, seed=3003)
+with knng.Context() as ctx:
+    k, d, st = ctx.build(x)
+h = hashlib.sha1()
+for t in (x, k, d):
+    h.update(t.contiguous().view(torch.uint8).cpu().numpy().tobytes())
+print("digest", h.hexdigest(), [int(st.updates[i]) for i in range(st.iterations)])
+"""
+
+
+def test_build_is_deterministic_across_processes(knng_mod):
+    """The same seeded rows give the same graph in separate processes (each
+    autotunes its join on its own clock, so the variant choice may differ):
+    400k rows generated on the GPU, built twice, in two child processes."""
+    import subprocess
+    import sys
+
+    pkg = os.path.join(os.path.dirname(HERE), "sisap-2026-task1_gb300")
+    outs = []
+    for _ in range(2):
+        r = subprocess.run([sys.executable, "-c", CHILD_BUILD.format(pkg=pkg)], capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0, r.stderr[-3000:]
+        outs.append([ln for ln in r.stdout.splitlines() if ln.startswith("digest")][-1])
+    assert outs[0] == outs[1], outs
+
+
 def test_build_natural_and_leaf_order_agree(knng_mod):
     knng = knng_mod
     x = synth.mixture(8000, 768, 80, seed=22)
