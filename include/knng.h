@@ -68,7 +68,7 @@ typedef struct knng_params {
   int device;            /* CUDA device ordinal */
   int autotune;          /* 1: time the join configurations once per (d, size) */
   int use_graph;         /* 1: replay the NN-Descent phase as a CUDA graph */
-  int gram_mode;         /* leaf Gram: KNNG_GRAM_DP4A or KNNG_GRAM_TCGEN05 (bf16 tensor cores) */
+  int gram_mode;         /* leaf Gram: KNNG_GRAM_DP4A or KNNG_GRAM_TCGEN05 (f16 tensor cores) */
   int init_mode;         /* KNNG_INIT_FOREST (src/main.cpp); KNNG_INIT_RANDOM, the archived
                             variant archive/nndescent_optimized.cpp:97-118 (needs n > k_build);
                             KNNG_INIT_BLOCK, the archived block-partitioned hybrid

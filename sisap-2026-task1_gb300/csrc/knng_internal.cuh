@@ -185,7 +185,7 @@ int run_init(const int8_t* codes, int64_t n, int d, int T, int leaf, int K, uint
              const int32_t* perm, const uint8_t* leaf_flag, int32_t* ids, int32_t* scores,
              const InitBufs& ib, cudaStream_t s, int64_t* leaves_out, std::string* err,
              const JobTable& jt, int gram_mode = 0, int wait_limit = 0);
-// gram_mode 0: dp4a leaf Gram (leaf_gram); 1: tcgen05 bf16 tensor-core Gram (leaf_gram_tc)
+// gram_mode 0: dp4a leaf Gram (leaf_gram); 1: tcgen05 f16 tensor-core Gram (leaf_gram_tc)
 // wait_limit: knng_params::wait_limit (0 = default polls per bounded wait)
 // Gram rows of the leaves [leaf_start, leaf_start + nleaves) (the last one ends
 // at position `total`) go to gram[(position - gram_pos0) * 64 ...].

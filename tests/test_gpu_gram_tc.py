@@ -1,6 +1,6 @@
-"""The tcgen05 (bf16 tensor-core) leaf Gram against the dp4a one and the oracle.
+"""The tcgen05 (f16 tensor-core) leaf Gram against the dp4a one and the oracle.
 
-int8 codes are exact in bf16 and every partial sum of a Gram entry is an
+int8 codes are exact in f16 and every partial sum of a Gram entry is an
 integer of magnitude <= d * 128^2 <= 2^24, exact in fp32, so the tensor-core
 Gram must reproduce the int32 dots bit for bit -- including rows of extreme
 codes (all -128: dot = 1024 * 16384 = 2^24 exactly) and leaves of every size.
