@@ -9,7 +9,7 @@
 // Here the dots come from one Gram block per leaf (K3: every member pair of a
 // <= 64-member leaf, read once from HBM into shared memory), and a warp per
 // row merges its T leaf rows into a sorted top-K list held two entries per
-// lane (K4).  The merge keeps the K best distinct (score desc, id asc) keys,
+// lane (K4), one batched merge per 32 candidates (merge_batch).  The merge keeps the K best distinct (score desc, id asc) keys,
 // which is the reference's pool order among equal scores (its pool is sorted
 // by id before the unstable partial_sort; ties are unspecified there and fixed
 // here).  Rows with fewer than K distinct candidates take the reference's
@@ -151,6 +151,55 @@ __device__ __forceinline__ uint64_t list_insert(uint64_t& kA, uint64_t& kB, uint
   return (K - 1) < 32 ? __shfl_sync(full, kA, K - 1) : __shfl_sync(full, kB, K - 33);
 }
 
+// Merge one leaf half's candidate keys (one per lane, 0 = none) into the
+// descending list kA/kB (positions lane and 32 + lane, length K; 0 = empty):
+// afterwards it holds the K best distinct keys of both.  One pass for all the
+// candidates above the threshold instead of one insertion each: the list goes
+// to the warp's shared-memory row; such a candidate finds its rank in the list
+// by binary search (an equal key is listed already) and its rank among the
+// other candidates by counting; every list entry moves down by the number of
+// candidates above it.  The ranks are a permutation of the merged order, so
+// each entry and candidate is written once, and those at rank >= K drop out.
+// Returns the new threshold (the K-th key, 0 while the list is not full).
+__device__ __forceinline__ uint64_t merge_batch(uint64_t& kA, uint64_t& kB, uint64_t key, uint64_t thr, int K,
+                                                int lane, uint64_t* sl) {
+  const unsigned full = 0xffffffffu;
+  bool want = key > thr;
+  if (!__any_sync(full, want)) return thr;
+  sl[lane] = kA;
+  sl[32 + lane] = kB;
+  __syncwarp();
+  int lo = 0;
+  if (want) {
+    int hi = K;  // first list position whose key is <= key
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (sl[mid] > key) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo < K && sl[lo] == key) want = false;
+  }
+  unsigned acc = __ballot_sync(full, want);
+  int above = 0, cA = 0, cB = 0;
+  while (acc) {
+    const int src = __ffs(acc) - 1;
+    acc &= acc - 1;
+    const uint64_t ck = __shfl_sync(full, key, src);
+    above += ck > key ? 1 : 0;
+    cA += ck > kA ? 1 : 0;
+    cB += ck > kB ? 1 : 0;
+  }
+  __syncwarp();
+  if (lane < K && lane + cA < K) sl[lane + cA] = kA;
+  if (32 + lane < K && 32 + lane + cB < K) sl[32 + lane + cB] = kB;
+  if (want && lo + above < K) sl[lo + above] = key;
+  __syncwarp();
+  kA = lane < K ? sl[lane] : 0;
+  kB = 32 + lane < K ? sl[32 + lane] : 0;
+  __syncwarp();  // the row is rewritten by the next merge
+  return (K - 1) < 32 ? __shfl_sync(full, kA, K - 1) : __shfl_sync(full, kB, K - 33);
+}
+
 // K4: one warp per row; merge the row's leaf Gram rows of trees [t0, t1) into
 // its top-K list.  The first chunk of trees starts from an empty list, later
 // chunks from the list the previous chunk wrote (keys round-trip exactly, and
@@ -167,6 +216,7 @@ __global__ void __launch_bounds__(256) init_merge(int64_t n, int t0, int t1, int
                                                   int64_t gram_rows, unsigned* err) {
   (void)gram_rows;
   (void)err;
+  __shared__ uint64_t s_list[8][kMaxK];  // one list row per warp (merge_batch)
   const int lane = threadIdx.x & 31;
   const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
   for (int64_t i = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
@@ -197,13 +247,7 @@ __global__ void __launch_bounds__(256) init_merge(int64_t n, int t0, int t1, int
         const int j = lane + 32 * half;
         uint64_t key = 0;
         if (j < m && j != self) key = make_key(grow[j], perm[s + j]);
-        unsigned acc = __ballot_sync(0xffffffffu, key > thr);
-        while (acc) {
-          const int src = __ffs(acc) - 1;
-          acc &= acc - 1;
-          const uint64_t ck = __shfl_sync(0xffffffffu, key, src);
-          if (ck > thr) thr = list_insert(kA, kB, ck, K, lane);
-        }
+        thr = merge_batch(kA, kB, key, thr, K, lane, s_list[threadIdx.x >> 5]);
       }
     }
     const int real = __popc(__ballot_sync(0xffffffffu, kA != 0)) + __popc(__ballot_sync(0xffffffffu, kB != 0));
