@@ -103,9 +103,10 @@ struct knng_ctx {
   // pageable caller memory goes through these pinned buffers, copied by host threads
   PinnedBuf pin_in, pin_out;
   std::unique_ptr<CopyPool> pool;
-  CopyPool& copier() {
-    if (!pool) pool.reset(new CopyPool(host_copy_threads()));
-    return *pool;
+  void host_copy(void* dst, const void* src, size_t bytes) {
+    if (!pool) pool.reset(new (std::nothrow) CopyPool(host_copy_threads()));
+    if (pool) pool->copy(dst, src, bytes);
+    else std::memcpy(dst, src, bytes);
   }
   cudaEvent_t itev[kMaxIterEvents] = {};
   std::string last_error;
@@ -283,6 +284,8 @@ int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_devic
     if (cudaPointerGetAttributes(&at, rows) == cudaSuccess) {
       if ((at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeManaged) && at.devicePointer)
         direct = static_cast<const float*>(at.devicePointer);
+      else if (at.type == cudaMemoryTypeDevice)  // device rows passed as host rows: read them in place
+        direct = static_cast<const float*>(rows);
     } else {
       cudaGetLastError();  // an unknown pointer is pageable memory
     }
@@ -307,7 +310,7 @@ int quantize_input(knng_ctx* c, const void* rows, int64_t n, int d, int on_devic
     const int64_t m = std::min<int64_t>(chunk_rows, n - off);
     const int b = int(k & 1);
     if ((e = cudaEventSynchronize(c->freed[b]))) return cuda_fail(c, e, "input staging");
-    c->copier().copy(c->pin_in.as<char>(b * chunk_bytes), src + off * d, size_t(m) * d * 4);
+    c->host_copy(c->pin_in.as<char>(b * chunk_bytes), src + off * d, size_t(m) * d * 4);
     if ((e = launch_quantize(slot_dev[b], m, d, c->prm.quant_mode, codes + off * d, sketch + off * W, c->stream)))
       return cuda_fail(c, e, "quantize");
     if ((e = cudaEventRecord(c->freed[b], c->stream))) return cuda_fail(c, e, "staging events");
@@ -656,8 +659,8 @@ int run_batch(knng_ctx* c, BJob* jobs, int J, int d, knng_stats& S) {
   for (int b = 0; b < J; ++b)
     if (via_pin[b]) {
       const size_t cnt_b = size_t(jobs[b].n) * p.k_eval, at = size_t(hoff[b]) * p.k_eval;
-      c->copier().copy(jobs[b].knns, c->pin_out.as<int32_t>(at * 4), cnt_b * 4);
-      c->copier().copy(jobs[b].dists, c->pin_out.as<float>((outn + at) * 4), cnt_b * 4);
+      c->host_copy(jobs[b].knns, c->pin_out.as<int32_t>(at * 4), cnt_b * 4);
+      c->host_copy(jobs[b].dists, c->pin_out.as<float>((outn + at) * 4), cnt_b * 4);
     }
   int max_it = 0;
   for (int b = 0; b < J; ++b) {

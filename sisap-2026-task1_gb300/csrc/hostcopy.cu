@@ -56,8 +56,16 @@ bool host_pageable(const void* ptr) {
   return at.type == cudaMemoryTypeUnregistered;
 }
 
-CopyPool::CopyPool(int threads) : nthreads_(std::max(1, threads)) {
-  for (int t = 1; t < nthreads_; ++t) workers_.emplace_back([this, t] { run(t); });
+CopyPool::CopyPool(int threads) : nthreads_(1) {
+  // a thread that cannot be started leaves the pool smaller (no exception
+  // leaves the library); the caller always copies slice 0 itself
+  try {
+    for (int t = 1; t < std::max(1, threads); ++t) {
+      workers_.emplace_back([this, t] { run(t); });
+      nthreads_ = t + 1;
+    }
+  } catch (...) {
+  }
 }
 
 CopyPool::~CopyPool() {

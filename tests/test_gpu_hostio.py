@@ -56,3 +56,31 @@ def test_batch_with_pageable_rows_equals_plain_builds():
             k1, d1, _ = ctx.build(x)
             np.testing.assert_array_equal(k, k1)
             np.testing.assert_array_equal(dd, d1)
+
+
+@pytest.mark.gpu
+def test_device_rows_passed_as_host_rows_are_read_in_place():
+    """A caller that passes device memory with rows_on_device = 0 gets the same
+    graph as with the flag set: the library looks at the pointer and reads
+    device rows in place instead of copying them as host memory."""
+    import ctypes as C
+
+    import torch
+
+    import knng
+
+    n, d = 20_000, 1024
+    x = synth.mixture(n, d, 200, seed=78)
+    xd = torch.from_numpy(x).cuda()
+    prm = knng.params(max_iterations=2)
+    with knng.Context(prm) as ctx:
+        k_ref, d_ref, _ = ctx.build(x)
+        k_out = np.empty((n, prm.k_eval), np.int32)
+        d_out = np.empty((n, prm.k_eval), np.float32)
+        torch.cuda.synchronize()
+        st = knng.Stats()
+        rc = knng.lib().knng_build(ctx.h, C.c_void_p(xd.data_ptr()), n, d, 0, k_out.ctypes.data_as(C.c_void_p),
+                                   d_out.ctypes.data_as(C.c_void_p), 0, C.byref(st))
+    assert rc == 0
+    np.testing.assert_array_equal(k_out, k_ref)
+    np.testing.assert_array_equal(d_out, d_ref)
