@@ -749,58 +749,60 @@ const char* knng_status_string(int s) {
 const char* knng_last_error(const knng_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
 
 int knng_create(knng_ctx** out, const knng_params* p) {
-  if (!out) return KNNG_E_ARGS;
-  *out = nullptr;
-  knng_ctx* c = new (std::nothrow) knng_ctx();
-  if (!c) return KNNG_E_OOM;
-  if (p) c->prm = *p; else knng_default_params(&c->prm);
-  int st = check_params(c, c->prm);
-  if (st) {
-    delete c;
-    return st;
-  }
-  cudaError_t e;
-  c->device = c->prm.device;
-  if ((e = cudaSetDevice(c->device)) ||
-      (e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device)) ||
-      (e = cudaDeviceGetAttribute(&c->pageable_access, cudaDevAttrPageableMemoryAccess, c->device)) ||
-      (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking))) {
-    delete c;
-    return KNNG_E_CUDA;
-  }
-  for (auto& ev : c->ev)
-    if ((e = cudaEventCreate(&ev))) {
+  return abi_guard(nullptr, [&]() -> int {
+    if (!out) return KNNG_E_ARGS;
+    *out = nullptr;
+    knng_ctx* c = new (std::nothrow) knng_ctx();
+    if (!c) return KNNG_E_OOM;
+    if (p) c->prm = *p; else knng_default_params(&c->prm);
+    int st = check_params(c, c->prm);
+    if (st) {
+      delete c;
+      return st;
+    }
+    cudaError_t e;
+    c->device = c->prm.device;
+    if ((e = cudaSetDevice(c->device)) ||
+        (e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device)) ||
+        (e = cudaDeviceGetAttribute(&c->pageable_access, cudaDevAttrPageableMemoryAccess, c->device)) ||
+        (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking))) {
+      delete c;
+      return KNNG_E_CUDA;
+    }
+    for (auto& ev : c->ev)
+      if ((e = cudaEventCreate(&ev))) {
+        knng_destroy(c);
+        return KNNG_E_CUDA;
+      }
+    for (auto& ev : c->jev)
+      if ((e = cudaEventCreate(&ev))) {
+        knng_destroy(c);
+        return KNNG_E_CUDA;
+      }
+    for (auto& ev : c->itev)
+      if ((e = cudaEventCreate(&ev))) {
+        knng_destroy(c);
+        return KNNG_E_CUDA;
+      }
+    if ((e = cudaEventCreate(&c->bev))) {
       knng_destroy(c);
       return KNNG_E_CUDA;
     }
-  for (auto& ev : c->jev)
-    if ((e = cudaEventCreate(&ev))) {
-      knng_destroy(c);
-      return KNNG_E_CUDA;
-    }
-  for (auto& ev : c->itev)
-    if ((e = cudaEventCreate(&ev))) {
-      knng_destroy(c);
-      return KNNG_E_CUDA;
-    }
-  if ((e = cudaEventCreate(&c->bev))) {
-    knng_destroy(c);
-    return KNNG_E_CUDA;
-  }
-  for (int k = 0; k < 2; ++k)
-    if ((e = cudaEventCreateWithFlags(&c->freed[k], cudaEventDisableTiming))) {
-      knng_destroy(c);
-      return KNNG_E_CUDA;
-    }
-  for (DevBuf* b : c->buffers()) b->s = c->stream;
-  // resolve the join kernels' launch attributes now, outside any capture
-  for (int d : {128, 256, 384, 512, 640, 768, 896, 1024})
-    if ((e = join_prepare_all(c->prm.k_build, c->prm.k_build * c->prm.rerank_mult, d))) {
-      c->last_error = std::string("join variants: ") + join_variant_error();
-      break;
-    }
-  *out = c;
-  return KNNG_OK;
+    for (int k = 0; k < 2; ++k)
+      if ((e = cudaEventCreateWithFlags(&c->freed[k], cudaEventDisableTiming))) {
+        knng_destroy(c);
+        return KNNG_E_CUDA;
+      }
+    for (DevBuf* b : c->buffers()) b->s = c->stream;
+    // resolve the join kernels' launch attributes now, outside any capture
+    for (int d : {128, 256, 384, 512, 640, 768, 896, 1024})
+      if ((e = join_prepare_all(c->prm.k_build, c->prm.k_build * c->prm.rerank_mult, d))) {
+        c->last_error = std::string("join variants: ") + join_variant_error();
+        break;
+      }
+    *out = c;
+    return KNNG_OK;
+  });
 }
 
 void knng_destroy(knng_ctx* c) {
@@ -849,73 +851,79 @@ int knng_sketch_hyperplane(const int8_t* codes_dev, int64_t n, int d, uint32_t s
 
 int knng_forest(knng_ctx* c, const int8_t* codes_dev, int64_t n, int d, const int32_t* replay, int64_t n_replay,
                 int32_t* perm_dev, uint8_t* leaf_flag_dev) {
-  if (!c || !codes_dev || !perm_dev || !leaf_flag_dev || (n_replay > 0 && !replay)) return KNNG_E_ARGS;
-  int st = check_shape(c, n, d);
-  if (st) return st;
-  cudaSetDevice(c->device);
-  Scratch s;
-  if ((st = ensure_scratch(c, n, &s, replay ? n_replay : 0))) return st;
-  int64_t levels = 0;
-  JobTable jt;
-  if ((st = single_job(c, n, &jt))) return st;
-  st = run_forest(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.seed, replay, replay ? n_replay : 0,
-                  perm_dev, leaf_flag_dev, s.fb, c->stream, &levels, &c->last_error, jt,
-                  n > c->prm.leaf_size ? 1 : 0, c->prm.forest_fuse);
-  if (st) return st;
-  cudaError_t e = cudaStreamSynchronize(c->stream);
-  return e ? cuda_fail(c, e, "forest") : KNNG_OK;
+  return abi_guard(c ? &c->last_error : nullptr, [&]() -> int {
+    if (!c || !codes_dev || !perm_dev || !leaf_flag_dev || (n_replay > 0 && !replay)) return KNNG_E_ARGS;
+    int st = check_shape(c, n, d);
+    if (st) return st;
+    cudaSetDevice(c->device);
+    Scratch s;
+    if ((st = ensure_scratch(c, n, &s, replay ? n_replay : 0))) return st;
+    int64_t levels = 0;
+    JobTable jt;
+    if ((st = single_job(c, n, &jt))) return st;
+    st = run_forest(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.seed, replay, replay ? n_replay : 0,
+                    perm_dev, leaf_flag_dev, s.fb, c->stream, &levels, &c->last_error, jt,
+                    n > c->prm.leaf_size ? 1 : 0, c->prm.forest_fuse);
+    if (st) return st;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    return e ? cuda_fail(c, e, "forest") : KNNG_OK;
+  });
 }
 
 int knng_init_graph(knng_ctx* c, const int8_t* codes_dev, int64_t n, int d, const int32_t* perm_dev,
                     const uint8_t* leaf_flag_dev, int32_t* ids_dev, int32_t* scores_dev) {
-  if (!c || !codes_dev || !perm_dev || !leaf_flag_dev || !ids_dev || !scores_dev) return KNNG_E_ARGS;
-  int st = check_shape(c, n, d);
-  if (st) return st;
-  cudaSetDevice(c->device);
-  Scratch s;
-  if ((st = ensure_scratch(c, n, &s, 0))) return st;
-  JobTable jt;
-  if ((st = single_job(c, n, &jt))) return st;
-  st = run_init(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.k_build, c->prm.seed, perm_dev,
-                leaf_flag_dev, ids_dev, scores_dev, s.ib, c->stream, nullptr, &c->last_error, jt, c->prm.gram_mode,
-                c->prm.wait_limit);
-  if (st) return st;
-  cudaError_t e = cudaStreamSynchronize(c->stream);
-  return e ? cuda_fail(c, e, "init") : KNNG_OK;
+  return abi_guard(c ? &c->last_error : nullptr, [&]() -> int {
+    if (!c || !codes_dev || !perm_dev || !leaf_flag_dev || !ids_dev || !scores_dev) return KNNG_E_ARGS;
+    int st = check_shape(c, n, d);
+    if (st) return st;
+    cudaSetDevice(c->device);
+    Scratch s;
+    if ((st = ensure_scratch(c, n, &s, 0))) return st;
+    JobTable jt;
+    if ((st = single_job(c, n, &jt))) return st;
+    st = run_init(codes_dev, n, d, c->prm.num_trees, c->prm.leaf_size, c->prm.k_build, c->prm.seed, perm_dev,
+                  leaf_flag_dev, ids_dev, scores_dev, s.ib, c->stream, nullptr, &c->last_error, jt, c->prm.gram_mode,
+                  c->prm.wait_limit);
+    if (st) return st;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    return e ? cuda_fail(c, e, "init") : KNNG_OK;
+  });
 }
 
 int knng_join_iter(knng_ctx* c, const int8_t* codes_dev, const uint64_t* sketch_dev, int64_t n, int d,
                    const int32_t* ids_in, const int32_t* scores_in, int32_t* ids_out, int32_t* scores_out,
                    int64_t* updates) {
-  if (!c || !codes_dev || !sketch_dev || !ids_in || !scores_in || !ids_out || !scores_out) return KNNG_E_ARGS;
-  if ((ids_out == ids_in) != (scores_out == scores_in)) return set_error(c, KNNG_E_ARGS, "mixed in-place buffers");
-  int st = check_shape(c, n, d);
-  if (st) return st;
-  cudaSetDevice(c->device);
-  cudaError_t e;
-  if ((e = c->scalars.ensure(4096))) return cuda_fail(c, e, "scalar allocation");
-  unsigned long long* up = c->scalars.as<unsigned long long>(256);
-  if ((e = cudaMemsetAsync(up, 0, 64, c->stream))) return cuda_fail(c, e, "update counter");
-  const int K = c->prm.k_build;
-  const int cps = c->prm.join_ctas_per_sm ? c->prm.join_ctas_per_sm : 4;
-  const int cb = c->prm.join_ctas_per_sm ? c->prm.join_cblock : 4;
-  JoinCtl chk{};  // no jobs, no cache, no row flags: only the bounds-checked build's error word
-  chk.check_err = kChecked ? c->scalars.as<unsigned>(kCheckWord) : nullptr;
-  if (kChecked && (e = cudaMemsetAsync(chk.check_err, 0, sizeof(unsigned), c->stream)))
-    return cuda_fail(c, e, "check word reset");
-  if ((e = launch_join(codes_dev, sketch_dev, n, d, K, K * c->prm.rerank_mult, ids_in, scores_in, ids_out,
-                       scores_out, nullptr, up, c->num_sms, c->stream, nullptr, kChecked ? &chk : nullptr, cps, cb,
-                       c->sketch_words(d))))
-    return cuda_fail(c, e, "join");
-  unsigned long long h = 0;
-  unsigned check = 0;
-  if ((e = cudaMemcpyAsync(&h, up, 8, cudaMemcpyDeviceToHost, c->stream))) return cuda_fail(c, e, "update count");
-  if (kChecked && (e = cudaMemcpyAsync(&check, chk.check_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream)))
-    return cuda_fail(c, e, "check word");
-  if ((e = cudaStreamSynchronize(c->stream))) return cuda_fail(c, e, "join");
-  if (check & kErrBounds) return set_error(c, KNNG_E_BOUNDS, "join: an id outside [0, n) (bounds check)");
-  if (updates) *updates = int64_t(h);
-  return KNNG_OK;
+  return abi_guard(c ? &c->last_error : nullptr, [&]() -> int {
+    if (!c || !codes_dev || !sketch_dev || !ids_in || !scores_in || !ids_out || !scores_out) return KNNG_E_ARGS;
+    if ((ids_out == ids_in) != (scores_out == scores_in)) return set_error(c, KNNG_E_ARGS, "mixed in-place buffers");
+    int st = check_shape(c, n, d);
+    if (st) return st;
+    cudaSetDevice(c->device);
+    cudaError_t e;
+    if ((e = c->scalars.ensure(4096))) return cuda_fail(c, e, "scalar allocation");
+    unsigned long long* up = c->scalars.as<unsigned long long>(256);
+    if ((e = cudaMemsetAsync(up, 0, 64, c->stream))) return cuda_fail(c, e, "update counter");
+    const int K = c->prm.k_build;
+    const int cps = c->prm.join_ctas_per_sm ? c->prm.join_ctas_per_sm : 4;
+    const int cb = c->prm.join_ctas_per_sm ? c->prm.join_cblock : 4;
+    JoinCtl chk{};  // no jobs, no cache, no row flags: only the bounds-checked build's error word
+    chk.check_err = kChecked ? c->scalars.as<unsigned>(kCheckWord) : nullptr;
+    if (kChecked && (e = cudaMemsetAsync(chk.check_err, 0, sizeof(unsigned), c->stream)))
+      return cuda_fail(c, e, "check word reset");
+    if ((e = launch_join(codes_dev, sketch_dev, n, d, K, K * c->prm.rerank_mult, ids_in, scores_in, ids_out,
+                         scores_out, nullptr, up, c->num_sms, c->stream, nullptr, kChecked ? &chk : nullptr, cps, cb,
+                         c->sketch_words(d))))
+      return cuda_fail(c, e, "join");
+    unsigned long long h = 0;
+    unsigned check = 0;
+    if ((e = cudaMemcpyAsync(&h, up, 8, cudaMemcpyDeviceToHost, c->stream))) return cuda_fail(c, e, "update count");
+    if (kChecked && (e = cudaMemcpyAsync(&check, chk.check_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream)))
+      return cuda_fail(c, e, "check word");
+    if ((e = cudaStreamSynchronize(c->stream))) return cuda_fail(c, e, "join");
+    if (check & kErrBounds) return set_error(c, KNNG_E_BOUNDS, "join: an id outside [0, n) (bounds check)");
+    if (updates) *updates = int64_t(h);
+    return KNNG_OK;
+  });
 }
 
 int knng_export(const int32_t* ids_dev, const int32_t* scores_dev, int64_t n, int k_build, int k_eval,
@@ -941,13 +949,15 @@ int knng_export(const int32_t* ids_dev, const int32_t* scores_dev, int64_t n, in
 
 int knng_build(knng_ctx* c, const void* rows, int64_t n, int d, int rows_on_device, int32_t* knns, float* dists,
                int out_on_device, knng_stats* stats) {
-  if (!c || !rows || !knns || !dists) return set_error(c, KNNG_E_ARGS, "null argument");
-  int st = check_shape(c, n, d);
-  if (st) return st;
-  cudaSetDevice(c->device);
-  BJob j{rows, n, rows_on_device, knns, dists, out_on_device, 0};
-  knng_stats local{};
-  return run_batch(c, &j, 1, d, stats ? *stats : local);
+  return abi_guard(c ? &c->last_error : nullptr, [&]() -> int {
+    if (!c || !rows || !knns || !dists) return set_error(c, KNNG_E_ARGS, "null argument");
+    int st = check_shape(c, n, d);
+    if (st) return st;
+    cudaSetDevice(c->device);
+    BJob j{rows, n, rows_on_device, knns, dists, out_on_device, 0};
+    knng_stats local{};
+    return run_batch(c, &j, 1, d, stats ? *stats : local);
+  });
 }
 
 int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on_device) {
@@ -973,108 +983,112 @@ int64_t knng_footprint_bytes(const knng_params* p, int64_t n, int d, int rows_on
 }
 
 int knng_trim(knng_ctx* c) {
-  if (!c) return KNNG_E_ARGS;
-  cudaSetDevice(c->device);
-  if (c->join_graph) {
-    cudaGraphExecDestroy(c->join_graph);
-    c->join_graph = nullptr;
-    c->join_graph_key.clear();
-  }
-  for (DevBuf* b : c->buffers()) b->release();
-  cudaStreamSynchronize(c->stream);  // no copy still reads or writes the pinned buffers
-  c->pin_in.release();
-  c->pin_out.release();
-  for (knng_ctx* sub : c->subs) knng_trim(sub);
-  return KNNG_OK;
+  return abi_guard(c ? &c->last_error : nullptr, [&]() -> int {
+    if (!c) return KNNG_E_ARGS;
+    cudaSetDevice(c->device);
+    if (c->join_graph) {
+      cudaGraphExecDestroy(c->join_graph);
+      c->join_graph = nullptr;
+      c->join_graph_key.clear();
+    }
+    for (DevBuf* b : c->buffers()) b->release();
+    cudaStreamSynchronize(c->stream);  // no copy still reads or writes the pinned buffers
+    c->pin_in.release();
+    c->pin_out.release();
+    for (knng_ctx* sub : c->subs) knng_trim(sub);
+    return KNNG_OK;
+  });
 }
 
 int knng_build_batch(knng_ctx* c, knng_job* jobs, int count, knng_stats* stats) {
-  if (!c || !jobs || count < 1) return set_error(c, KNNG_E_ARGS, "null argument or empty batch");
-  for (int b = 0; b < count; ++b) {
-    if (!jobs[b].rows || !jobs[b].knns || !jobs[b].dists) return set_error(c, KNNG_E_ARGS, "null job buffer");
-    int st = check_shape(c, jobs[b].n, jobs[b].d);
-    if (st) return st;
-  }
-  cudaSetDevice(c->device);
-  knng_stats local{};
-  knng_stats& S = stats ? *stats : local;
-  std::memset(&S, 0, sizeof(S));
-  // one problem per dimension: jobs of equal d are laid out back to back; the
-  // groups run concurrently, each on its own context and stream
-  std::vector<int> dims;
-  for (int b = 0; b < count; ++b)
-    if (std::find(dims.begin(), dims.end(), jobs[b].d) == dims.end()) dims.push_back(jobs[b].d);
-  const int G = int(dims.size());
-  while (int(c->subs.size()) < G - 1) {
-    knng_ctx* sub = nullptr;
-    const int st = knng_create(&sub, &c->prm);
-    if (st) return set_error(c, st, "context for a dimension group");
-    c->subs.push_back(sub);
-  }
-  std::vector<std::vector<BJob>> groups(G);
-  std::vector<std::vector<int>> idx(G);
-  for (int g = 0; g < G; ++g)
+  return abi_guard(c ? &c->last_error : nullptr, [&]() -> int {
+    if (!c || !jobs || count < 1) return set_error(c, KNNG_E_ARGS, "null argument or empty batch");
+    for (int b = 0; b < count; ++b) {
+      if (!jobs[b].rows || !jobs[b].knns || !jobs[b].dists) return set_error(c, KNNG_E_ARGS, "null job buffer");
+      int st = check_shape(c, jobs[b].n, jobs[b].d);
+      if (st) return st;
+    }
+    cudaSetDevice(c->device);
+    knng_stats local{};
+    knng_stats& S = stats ? *stats : local;
+    std::memset(&S, 0, sizeof(S));
+    // one problem per dimension: jobs of equal d are laid out back to back; the
+    // groups run concurrently, each on its own context and stream
+    std::vector<int> dims;
     for (int b = 0; b < count; ++b)
-      if (jobs[b].d == dims[g]) {
-        groups[g].push_back(BJob{jobs[b].rows, jobs[b].n, jobs[b].rows_on_device, jobs[b].knns, jobs[b].dists,
-                                 jobs[b].out_on_device, 0});
-        idx[g].push_back(b);
+      if (std::find(dims.begin(), dims.end(), jobs[b].d) == dims.end()) dims.push_back(jobs[b].d);
+    const int G = int(dims.size());
+    while (int(c->subs.size()) < G - 1) {
+      knng_ctx* sub = nullptr;
+      const int st = knng_create(&sub, &c->prm);
+      if (st) return set_error(c, st, "context for a dimension group");
+      c->subs.push_back(sub);
+    }
+    std::vector<std::vector<BJob>> groups(G);
+    std::vector<std::vector<int>> idx(G);
+    for (int g = 0; g < G; ++g)
+      for (int b = 0; b < count; ++b)
+        if (jobs[b].d == dims[g]) {
+          groups[g].push_back(BJob{jobs[b].rows, jobs[b].n, jobs[b].rows_on_device, jobs[b].knns, jobs[b].dists,
+                                   jobs[b].out_on_device, 0});
+          idx[g].push_back(b);
+        }
+    std::vector<knng_stats> gs(G);
+    std::vector<int> gst(G, KNNG_OK);
+    cudaEventRecord(c->bev, c->stream);  // batch start: every group's stream waits for it
+    auto run_group = [&](int g) {
+      knng_ctx* gc = g == 0 ? c : c->subs[size_t(g - 1)];
+      cudaSetDevice(gc->device);
+      cudaStreamWaitEvent(gc->stream, c->bev, 0);
+      gst[g] = run_batch(gc, groups[g].data(), int(groups[g].size()), dims[g], gs[g]);
+      if (gst[g] && gc != c) c->last_error = gc->last_error;
+    };
+    if (G == 1) {
+      run_group(0);
+    } else {
+      std::vector<std::thread> th;
+      for (int g = 1; g < G; ++g) th.emplace_back(run_group, g);
+      run_group(0);
+      for (auto& t : th) t.join();
+    }
+    float span_ms = 0.f;
+    for (int g = 0; g < G; ++g) {
+      knng_ctx* gc = g == 0 ? c : c->subs[size_t(g - 1)];
+      for (size_t q = 0; q < groups[g].size(); ++q) {
+        jobs[idx[g][q]].status = gst[g];
+        jobs[idx[g][q]].iterations = groups[g][q].iterations;
       }
-  std::vector<knng_stats> gs(G);
-  std::vector<int> gst(G, KNNG_OK);
-  cudaEventRecord(c->bev, c->stream);  // batch start: every group's stream waits for it
-  auto run_group = [&](int g) {
-    knng_ctx* gc = g == 0 ? c : c->subs[size_t(g - 1)];
-    cudaSetDevice(gc->device);
-    cudaStreamWaitEvent(gc->stream, c->bev, 0);
-    gst[g] = run_batch(gc, groups[g].data(), int(groups[g].size()), dims[g], gs[g]);
-    if (gst[g] && gc != c) c->last_error = gc->last_error;
-  };
-  if (G == 1) {
-    run_group(0);
-  } else {
-    std::vector<std::thread> th;
-    for (int g = 1; g < G; ++g) th.emplace_back(run_group, g);
-    run_group(0);
-    for (auto& t : th) t.join();
-  }
-  float span_ms = 0.f;
-  for (int g = 0; g < G; ++g) {
-    knng_ctx* gc = g == 0 ? c : c->subs[size_t(g - 1)];
-    for (size_t q = 0; q < groups[g].size(); ++q) {
-      jobs[idx[g][q]].status = gst[g];
-      jobs[idx[g][q]].iterations = groups[g][q].iterations;
+      if (gst[g] == KNNG_OK) span_ms = std::max(span_ms, elapsed(c->bev, gc->ev[5]));
     }
-    if (gst[g] == KNNG_OK) span_ms = std::max(span_ms, elapsed(c->bev, gc->ev[5]));
-  }
-  for (int g = 0; g < G; ++g)
-    if (gst[g]) return gst[g];
-  for (int g = 0; g < G; ++g) {
-    S.quantize_s += gs[g].quantize_s;
-    S.forest_s += gs[g].forest_s;
-    S.init_s += gs[g].init_s;
-    S.join_s += gs[g].join_s;
-    S.export_s += gs[g].export_s;
-    S.build_s += gs[g].build_s;
-    S.kernel_launches += gs[g].kernel_launches;
-    S.forest_levels = std::max(S.forest_levels, gs[g].forest_levels);
-    S.leaves += gs[g].leaves;
-    S.iterations = std::max(S.iterations, gs[g].iterations);
-    for (int it = 0; it < 64; ++it) {
-      S.updates[it] += gs[g].updates[it];
-      S.join_ms[it] += gs[g].join_ms[it];
-      S.join_candidates[it] += gs[g].join_candidates[it];
-      S.join_dots[it] += gs[g].join_dots[it];
-      S.join_distinct[it] += gs[g].join_distinct[it];
-      S.join_skipped[it] += gs[g].join_skipped[it];
+    for (int g = 0; g < G; ++g)
+      if (gst[g]) return gst[g];
+    for (int g = 0; g < G; ++g) {
+      S.quantize_s += gs[g].quantize_s;
+      S.forest_s += gs[g].forest_s;
+      S.init_s += gs[g].init_s;
+      S.join_s += gs[g].join_s;
+      S.export_s += gs[g].export_s;
+      S.build_s += gs[g].build_s;
+      S.kernel_launches += gs[g].kernel_launches;
+      S.forest_levels = std::max(S.forest_levels, gs[g].forest_levels);
+      S.leaves += gs[g].leaves;
+      S.iterations = std::max(S.iterations, gs[g].iterations);
+      for (int it = 0; it < 64; ++it) {
+        S.updates[it] += gs[g].updates[it];
+        S.join_ms[it] += gs[g].join_ms[it];
+        S.join_candidates[it] += gs[g].join_candidates[it];
+        S.join_dots[it] += gs[g].join_dots[it];
+        S.join_distinct[it] += gs[g].join_distinct[it];
+        S.join_skipped[it] += gs[g].join_skipped[it];
+      }
+      S.join_ctas_per_sm = gs[g].join_ctas_per_sm;
+      S.join_cblock = gs[g].join_cblock;
+      S.graph_used = gs[g].graph_used;
     }
-    S.join_ctas_per_sm = gs[g].join_ctas_per_sm;
-    S.join_cblock = gs[g].join_cblock;
-    S.graph_used = gs[g].graph_used;
-  }
-  // stage sums add up the groups' own times; device_s is the batch's span
-  S.device_s = span_ms * 1e-3;
-  return KNNG_OK;
+    // stage sums add up the groups' own times; device_s is the batch's span
+    S.device_s = span_ms * 1e-3;
+    return KNNG_OK;
+  });
 }
 
 }  // extern "C"

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -46,6 +47,28 @@ constexpr bool kChecked = false;
 #endif
 
 inline bool dim_ok(int d) { return d >= 128 && d <= kMaxDim && d % 128 == 0; }
+
+// Runs an entry point's body and turns a C++ exception into a status, so none
+// crosses the C ABI: std::bad_alloc -> KNNG_E_OOM, anything else ->
+// KNNG_E_CUDA; `note` (may be null) receives a short message.
+template <class F>
+int abi_guard(std::string* note, F&& body) noexcept {
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    try {
+      if (note) *note = "host memory allocation failed";
+    } catch (...) {
+    }
+    return KNNG_E_OOM;
+  } catch (...) {
+    try {
+      if (note) *note = "internal error (C++ exception)";
+    } catch (...) {
+    }
+    return KNNG_E_CUDA;
+  }
+}
 
 // Host-side count of kernels this library has launched (all contexts).
 int64_t launches();

@@ -137,7 +137,13 @@ extern "C" int knng_pca(const float* rows, int64_t n, int d, int dims, int devic
       break;
     }
     {
-      std::vector<float> one(static_cast<size_t>(n), 1.0f);
+      std::vector<float> one;
+      try {  // no exception leaves the library
+        one.assign(static_cast<size_t>(n), 1.0f);
+      } catch (...) {
+        rc = KNNG_E_OOM;
+        break;
+      }
       if (cudaMemcpy(ones, one.data(), size_t(n) * 4, cudaMemcpyHostToDevice)) {
         rc = KNNG_E_CUDA;
         break;
@@ -172,7 +178,13 @@ extern "C" int knng_pca(const float* rows, int64_t n, int d, int dims, int devic
       break;
     }
     int hinfo = 0;
-    std::vector<float> hw(static_cast<size_t>(d));
+    std::vector<float> hw;
+    try {
+      hw.resize(static_cast<size_t>(d));
+    } catch (...) {
+      rc = KNNG_E_OOM;
+      break;
+    }
     if (cudaMemcpy(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost) ||
         cudaMemcpy(hw.data(), w, size_t(d) * 4, cudaMemcpyDeviceToHost) || hinfo != 0) {
       rc = KNNG_E_CUDA;

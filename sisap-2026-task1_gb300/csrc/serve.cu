@@ -67,8 +67,18 @@ namespace {
 void worker_loop(knng_server* sv, int slot) {
   knng_ctx* ctx = sv->ctxs[size_t(slot)];
   const int64_t budget = int64_t(sv->prm.mem_budget_gb * 1e9);
+  // the only host allocations of the loop, made once: nothing below can throw
+  std::vector<uint64_t> batch;
+  std::vector<knng_job> jobs;
+  try {
+    batch.reserve(size_t(sv->prm.max_batch_jobs));
+    jobs.reserve(size_t(sv->prm.max_batch_jobs));
+  } catch (...) {
+    return;  // this slot stays idle; the others serve the queue
+  }
   for (;;) {
-    std::vector<uint64_t> batch;
+    batch.clear();
+    jobs.clear();
     int64_t fp = 0;
     {
       std::unique_lock<std::mutex> lk(sv->mu);
@@ -120,7 +130,6 @@ void worker_loop(knng_server* sv, int slot) {
       const auto now = clk::now();
       for (uint64_t id : batch) sv->tickets[id].started = now;
     }
-    std::vector<knng_job> jobs;
     {
       std::lock_guard<std::mutex> lk(sv->mu);
       for (uint64_t id : batch) jobs.push_back(sv->tickets[id].job);
@@ -181,6 +190,13 @@ int knng_server_create(knng_server** out, const knng_server_params* p) {
     delete sv;
     return KNNG_E_ARGS;
   }
+  try {
+    sv->ctxs.reserve(size_t(sv->prm.slots));
+    sv->workers.reserve(size_t(sv->prm.slots));
+  } catch (...) {
+    delete sv;
+    return KNNG_E_OOM;
+  }
   for (int s = 0; s < sv->prm.slots; ++s) {
     knng_ctx* c = nullptr;
     const int st = knng_create(&c, &sv->prm.build);
@@ -191,7 +207,19 @@ int knng_server_create(knng_server** out, const knng_server_params* p) {
     }
     sv->ctxs.push_back(c);
   }
-  for (int s = 0; s < sv->prm.slots; ++s) sv->workers.emplace_back(worker_loop, sv, s);
+  try {
+    for (int s = 0; s < sv->prm.slots; ++s) sv->workers.emplace_back(worker_loop, sv, s);
+  } catch (...) {  // a worker thread could not start: stop the ones that did
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    for (auto& t : sv->workers) t.join();
+    for (knng_ctx* c : sv->ctxs) knng_destroy(c);
+    delete sv;
+    return KNNG_E_CUDA;
+  }
   *out = sv;
   return KNNG_OK;
 }
@@ -203,14 +231,22 @@ int knng_submit(knng_server* sv, const knng_job* job, uint64_t* ticket) {
   t.job = *job;
   t.footprint = knng_footprint_bytes(&sv->prm.build, job->n, job->d, job->rows_on_device);
   t.submitted = clk::now();
-  {
+  const int st = knng::abi_guard(nullptr, [&]() -> int {
     std::lock_guard<std::mutex> lk(sv->mu);
-    *ticket = sv->next_ticket++;
-    sv->tickets.emplace(*ticket, t);
-    sv->queue.push_back(*ticket);
-  }
-  sv->cv_work.notify_one();
-  return KNNG_OK;
+    const uint64_t id = sv->next_ticket;
+    auto ins = sv->tickets.emplace(id, t);
+    try {
+      sv->queue.push_back(id);
+    } catch (...) {
+      sv->tickets.erase(ins.first);
+      throw;
+    }
+    ++sv->next_ticket;
+    *ticket = id;
+    return KNNG_OK;
+  });
+  if (st == KNNG_OK) sv->cv_work.notify_one();
+  return st;
 }
 
 int knng_poll(knng_server* sv, uint64_t ticket, knng_result* r) {
