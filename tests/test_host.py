@@ -95,6 +95,38 @@ def test_synth_is_deterministic():
     np.testing.assert_allclose(np.linalg.norm(a, axis=1), 1.0, atol=1e-5)
 
 
+def test_torch_mixture_is_reproducible_and_seeded():
+    """The bench's generator: the same arguments give the same rows (labels from
+    numpy's PCG64, centres and noise from a seeded torch generator), another
+    seed gives other rows, and every row is a unit vector."""
+    import torch
+
+    import synth
+
+    a = synth.mixture_torch(3000, 128, 40, seed=11, device="cpu", chunk=1000)
+    b = synth.mixture_torch(3000, 128, 40, seed=11, device="cpu", chunk=1000)
+    c = synth.mixture_torch(3000, 128, 40, seed=12, device="cpu", chunk=1000)
+    assert torch.equal(a, b) and not torch.equal(a, c)
+    torch.testing.assert_close(a.norm(dim=1), torch.ones(3000), atol=1e-5, rtol=0)
+
+
+def test_bench_arms_print_the_same_config():
+    """bench.py's GPU arm and reference arm name one configuration, so their
+    lines compare like for like (the reference arm times a bounded sample of it)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    class P:  # the library's default parameters, as knng.params() returns them
+        k_eval, k_build, num_trees, leaf_size, rerank_mult = 15, 50, 16, 64, 8
+
+    for name in bench.CONFIGS:
+        for ws in (1, 8):
+            assert bench.workload_config(name, ws, P()) == bench.workload_config(name, ws)
+
+
 def test_recall_matches_evaluator_definition():
     import synth
 
